@@ -389,18 +389,23 @@ int or_erode_dilate_nl(int pt, int rank, const int64_t *shape, const void *in, v
   return rc;
 }
 
-/* One static-SE pass, t_Dilate/t_Erode view switch (ero_dil_static_se_t.hpp:922-1126).
- * SESquare3D / SECross3D go through the slice-wise specialisations (:761-915), which read
- * the buffer as ibd[2] slices of ibd[0]*ibd[1] contiguous pixels laid out as ibd[0] rows of
- * ibd[1] pixels (:778-780, t_3DCopyOneSliceTo2D :80-96): i.e. as a row-major
- * (d2, d0, d1) volume.  That reading is reproduced here. */
+/* One static-SE pass, t_Dilate/t_Erode view switch (ero_dil_static_se_t.hpp:922-1126):
+ * the window of the SE's offsets, clipped at the image border.
+ *
+ * SESquare3D / SECross3D: the reference routes these through slice-wise
+ * specialisations (:761-915) that (1) read the buffer as ibd[2] slices of ibd[0] x ibd[1]
+ * pixels and (2) keep raw pointers ptmp1..3/ptmpL to slice buffers whose storage is then
+ * exchanged by imtmp.swap(...) and copy-assignments (:801-834), so from the second slice
+ * on they write unrelated slices (on random data even a 3x3x3 volume differs; their own
+ * test uses identical slices).  This restatement follows the SE's definition instead,
+ * which is also what the reference's neighbour-list path computes with the predefined
+ * se::SESquare3D / se::SECross3D (ero_dil_runtime_nl_se_t.hpp:54-96). */
 static int static_pass(int pt, int rank, const int64_t *shape, const void *in, void *out, int se,
                        int dilate) {
   const off3 *tab; int n = se_table(se, &tab);
   if (n < 0 || se_rank(se) != rank) return -3;
   int64_t d[3];
   if (dims3(rank, shape, d) < 0) return -1;
-  if (se == SE_SQUARE3D || se == SE_CROSS3D) { d[0] = shape[2]; d[1] = shape[0]; d[2] = shape[1]; }
 #define CALL_S(T, S) gather_##S(d, (const T *)in, (T *)out, tab, n, dilate)
   DISPATCH(pt, CALL_S)
   return 0;

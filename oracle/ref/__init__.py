@@ -1,0 +1,105 @@
+"""ctypes access to poutre2's own implementation (oracle/_ref/libpoutre_ref.so).
+
+TEST INFRASTRUCTURE ONLY: used to cross-check the C restatement on random inputs and
+as the timed CPU baseline.  ``available()`` is False when the library was not built
+(poutre2 sources neither mounted nor staged)."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .. import PTYPE, SE, OracleError
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(os.path.dirname(_HERE), "_ref", "libpoutre_ref.so")
+_lib = None
+
+
+def build():
+    from . import build_ref
+    return build_ref.build()
+
+
+def available() -> bool:
+    return os.path.exists(LIB)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not available():
+            raise OracleError("oracle/_ref/libpoutre_ref.so not built")
+        L = ctypes.CDLL(LIB)
+        P, I, I64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+        L.ref_last_error.restype = ctypes.c_char_p
+        L.ref_erode_dilate_static.argtypes = [I, I, P, P, P, I, I, I]
+        L.ref_erode_dilate_nl.argtypes = [I, I, P, P, P, P, I, I]
+        L.ref_line.argtypes = [I, I, P, P, P, I64, I, I]
+        L.ref_reconstruct.argtypes = [I, I, P, P, P, P, I, I]
+        L.ref_extrema.argtypes = [I, I, I, P, P, P, D, I]
+        L.ref_h_maxima_binary.argtypes = [I, P, P, P, D, I]
+        L.ref_leveling.argtypes = [I, I, I, P, P, P, P, I]
+        _lib = L
+    return _lib
+
+
+def _chk(rc):
+    if rc != 0:
+        raise OracleError("reference threw: " + lib().ref_last_error().decode())
+
+
+def _shape(a):
+    return (ctypes.c_int64 * 3)(*(list(a.shape) + [0] * (3 - a.ndim)))
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def erode_dilate_static(img, se, iterations=1, dilate=True):
+    a = np.ascontiguousarray(img); out = np.empty_like(a)
+    _chk(lib().ref_erode_dilate_static(PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se], iterations, int(dilate)))
+    return out
+
+
+def erode_dilate_nl(img, offsets, dilate=True):
+    a = np.ascontiguousarray(img); out = np.empty_like(a)
+    o = np.ascontiguousarray(np.array(offsets, dtype=np.int32).reshape(-1, a.ndim))
+    _chk(lib().ref_erode_dilate_nl(PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), _p(o), len(o), int(dilate)))
+    return out
+
+
+def line(img, half, axis="x", dilate=True):
+    a = np.ascontiguousarray(img); out = np.empty_like(a)
+    _chk(lib().ref_line(PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), half, 0 if axis == "x" else 1, int(dilate)))
+    return out
+
+
+def reconstruct(marker, mask, se="SESquare2D", dilate=True):
+    m = np.ascontiguousarray(marker); k = np.ascontiguousarray(mask); out = np.empty_like(m)
+    _chk(lib().ref_reconstruct(PTYPE[m.dtype], m.ndim, _shape(m), _p(m), _p(k), _p(out), SE[se], int(dilate)))
+    return out
+
+
+_EXTREMA = ["h_minima", "h_maxima", "h_concave", "h_convex", "dynamic_pseudo_opening", "dynamic_pseudo_closing"]
+
+
+def extrema(kind, img, h, se="SESquare2D"):
+    a = np.ascontiguousarray(img); out = np.empty_like(a)
+    _chk(lib().ref_extrema(_EXTREMA.index(kind), PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), float(h), SE[se]))
+    return out
+
+
+def h_maxima_binary(img, h, se="SESquare2D"):
+    a = np.ascontiguousarray(img, dtype=np.uint8); out = np.empty_like(a)
+    _chk(lib().ref_h_maxima_binary(a.ndim, _shape(a), _p(a), _p(out), float(h), SE[se]))
+    return out
+
+
+def leveling(kind, ref, marker, se="SESquare2D"):
+    r = np.ascontiguousarray(ref); m = np.ascontiguousarray(marker); out = np.empty_like(r)
+    k = {"low_leveling": 0, "high_leveling": 1, "leveling": 2}[kind]
+    _chk(lib().ref_leveling(k, PTYPE[r.dtype], r.ndim, _shape(r), _p(r), _p(m), _p(out), SE[se]))
+    return out
