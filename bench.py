@@ -1,0 +1,314 @@
+"""Benchmark of the GB300 morphology + geodesy path.
+
+Headline workload (one "step"): the binary h-maxima chain of a 2048x2048 uint8 image --
+white noise (seed 1), Gaussian sigma=4, rescaled to [0,255]; marker = sat_sub(mask, 20);
+geodesic reconstruction by dilation, 8-connectivity, to idempotence; output mask > rec as a
+binary uint8 image -- in one fused persistent launch.  Metric: Gpixel/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--extra]
+
+--impl reference times poutre2's own CPU implementation of the same workload (oracle/_ref,
+compiled from the reference sources; the C restatement if that library cannot be built) on
+the host cores.  Under torchrun (N > 1) every rank runs an independent replica (the images
+are independent; no collective on the data path), timing is max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Gpixel/s & %HBM peak: erode/dilate, reconstruction; ragged batch vs plain"
+UNIT = "Gpixel/s"
+H_VALUE = 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_for(key):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get(key)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_image(size):
+    from poutre2_gb300 import synthetic
+    return synthetic.smoothed_noise_u8((size, size), seed=1, sigma=4.0)
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_hmaxima(f, budget_s=12.0, min_runs=1):
+    """Time poutre2's CPU implementation (oracle/_ref) or, failing that, the C restatement on
+    `f`; returns (pixels/s, kind, runs)."""
+    import numpy as np
+    kind = "port"
+    fn = None
+    try:
+        from oracle import ref
+        if not ref.available():
+            try:
+                ref.build()
+            except Exception:
+                pass
+        if ref.available():
+            fn = lambda: ref.h_maxima_binary(f, H_VALUE, "SESquare2D")  # noqa: E731
+            kind = "reference"
+    except Exception:
+        fn = None
+    if fn is None:
+        import oracle
+        fn = lambda: oracle.h_maxima_binary(f, H_VALUE, "SESquare2D")  # noqa: E731
+    fn()  # warm
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < min_runs or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        fn()
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 50:
+            break
+    return f.size / statistics.median(times), kind, len(times)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    f = workload_image(args.size)
+    steps = []
+    for _ in range(args.warmup):
+        cpu_hmaxima(f, budget_s=0.0)
+    for _ in range(args.steps):
+        v, kind, runs = cpu_hmaxima(f, budget_s=0.0)
+        steps.append(1.0 / v * f.size)
+    t = statistics.mean(steps)
+    value = f.size / t / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": f"binary h-maxima (sat_sub h={H_VALUE}, reconstruction by dilation 8-conn, mask>rec) "
+                                   f"{args.size}x{args.size} u8 smoothed noise sigma=4 seed 1"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
+                             "sample": f"{args.steps} full runs of the {args.size}^2 workload, single thread "
+                                       f"(poutre2 has no threading)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def extra_measurements(dev, flush):
+    return {}
+
+
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from poutre2_gb300 import _lib, geo
+    from poutre2_gb300.se import Common_NL_SE
+    _lib.load()
+    geo.sync_checks = False
+
+    f = workload_image(args.size)
+    N = f.size
+    dev = torch.device("cuda", local)
+    x = torch.from_numpy(f).to(dev)
+    out = torch.empty_like(x)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        geo.h_maxima_binary(x, H_VALUE, Common_NL_SE.SESquare2D, out, check=False)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _lib.call("pg_check_device", None)
+    rounds = geo.last_reconstruction_rounds()
+
+    # device-resident timed region: per-step events, L2 flushed between steps (untimed)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush_l2(flush)
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t_step = sum(ms) / len(ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    _lib.call("pg_check_device", None)
+    value = ws * N / t_step / 1e9
+
+    # parity of the timed output against the oracle (outside the timed region)
+    import oracle
+    parity = bool(np.array_equal(out.cpu().numpy(), oracle.h_maxima_binary(f, H_VALUE, "SESquare2D")))
+
+    # end to end through the public API: pinned host input -> device -> result -> pinned host
+    hin = torch.from_numpy(f).pin_memory()
+    hout = torch.empty(f.shape, dtype=torch.uint8).pin_memory()
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        flush_l2(flush)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        xd = hin.to(dev, non_blocking=True)
+        od = torch.empty_like(xd)
+        geo.h_maxima_binary(xd, H_VALUE, Common_NL_SE.SESquare2D, od, check=False)
+        hout.copy_(od, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append(a.elapsed_time(b))
+    t_e2e = sum(e2e_ms) / len(e2e_ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+
+    peak, peak_kind = peaks()
+    alg_bytes = 2 * N  # mask read + binary output written, per launch
+    achieved = alg_bytes / t_step / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"binary h-maxima (sat_sub h={H_VALUE}, reconstruction by dilation 8-conn to "
+                               f"idempotence, mask>rec) {args.size}x{args.size} u8 smoothed noise sigma=4 seed 1",
+                   "l2": "flushed between timed steps (256 MB write, untimed)", "rounds": rounds,
+                   "parallelism": f"replicas x{ws}"},
+        "parity_vs_oracle": parity,
+        "e2e": {"value": ws * N / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(N), "d2h_bytes_per_step": int(N)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic_for(f"k_reconstruct@hmaxima{args.size}"),
+                     "peak_source": f"{peak_kind} hbm_gbs (burst)", "kernel": "k_reconstruct<u8,dilate,8-conn>",
+                     "algorithmic_bytes_per_launch": alg_bytes},
+        "gpu_launches": args.steps,  # one persistent k_reconstruct launch per step (plus one memset)
+        "clocks": clocks,
+    }
+    if rank == 0:
+        v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
+                                "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
+                                          f"(poutre2 is single-threaded)"}
+        if args.extra:
+            line["extra"] = extra_measurements(dev, flush)
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--extra", action="store_true", help="also measure the other workloads")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

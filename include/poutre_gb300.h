@@ -1,0 +1,218 @@
+/*
+ * poutre_gb300.h -- C ABI of the GB300 (sm_103a) morphology + geodesy library.
+ *
+ * This is the drop-in boundary for poutre2's low_level_morpho and geodesy entry points:
+ * each function below replaces one reference entry point (cited beside it, paths relative
+ * to the poutre2 source tree) with the same argument meaning, on device images.
+ *
+ * Conventions
+ *   - Images are dense, row-major, last dimension fastest, in device memory owned by the
+ *     caller (poutre::details::image_t layout, array_view.hpp:908-912).  shape[] holds the
+ *     reference's dimensions {d0, .., d_{rank-1}}, d0 slowest.
+ *   - ptype values are poutre::PType's (include/poutre/base/types.hpp:517-526); uint16 is
+ *     an addition (PG_PTYPE_U16).
+ *   - Every call is asynchronous on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream) and returns a status; no exception crosses the ABI.  Where the reference
+ *     throws std::runtime_error, the call returns the matching status and
+ *     pg_last_error() (thread-local) holds the message.
+ *   - Outputs must be distinct from inputs (AssertImagesAreDifferent,
+ *     src/base/image_interface.cpp:52-56,74-80); sizes and types must match
+ *     (AssertSizesCompatible / AssertAsTypesCompatible).
+ *   - Temporaries are taken from the device's stream-ordered pool (cudaMallocAsync)
+ *     on `stream`, as the reference allocates its own temporaries.
+ */
+#ifndef POUTRE_GB300_H
+#define POUTRE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define PG_API __declspec(dllexport)
+#else
+#define PG_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *pg_stream_t; /* == cudaStream_t */
+
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad rank/shape, negative iter, bad scalar  */
+  PG_ERR_UNSUPPORTED_PTYPE = 2, /* "unsupported PTYPE"                                      */
+  PG_ERR_UNSUPPORTED_SE = 3,    /* "unsupported nl_static" / SE rank differs from image rank */
+  PG_ERR_INCOMPATIBLE = 4,      /* sizes or types of the images differ                      */
+  PG_ERR_ALIASING = 5,          /* output is one of the inputs                              */
+  PG_ERR_NOT_SQUARE = 6,        /* DilateY/ErodeY on a non-square image (the reference throws) */
+  PG_ERR_CUDA = 7,              /* a CUDA runtime error (message in pg_last_error)          */
+  PG_ERR_OUT_OF_MEMORY = 8,     /* a temporary could not be allocated                       */
+  PG_ERR_NOT_CONVERGED = 9      /* reconstruction hit its round cap or a device wait limit  */
+} pg_status;
+
+typedef enum pg_ptype {
+  PG_PTYPE_U8 = 4,
+  PG_PTYPE_I32 = 8,
+  PG_PTYPE_F32 = 16,
+  PG_PTYPE_I64 = 32,
+  PG_PTYPE_F64 = 64,
+  PG_PTYPE_U16 = 128
+} pg_ptype;
+
+/* poutre::se::Common_NL_SE, include/poutre/structuring_element/se_types_and_tags.hpp:45-57 */
+typedef enum pg_common_se {
+  PG_SE_UNDEF = 0,
+  PG_SE_SEGMENT_X_1D = 1,
+  PG_SE_SQUARE_2D = 2,
+  PG_SE_CROSS_2D = 3,
+  PG_SE_SEGMENT_X_2D = 4,
+  PG_SE_SEGMENT_Y_2D = 5,
+  PG_SE_SEGMENT_X_3D = 6,
+  PG_SE_SEGMENT_Y_3D = 7,
+  PG_SE_SEGMENT_Z_3D = 8,
+  PG_SE_CROSS_3D = 9,
+  PG_SE_SQUARE_3D = 10
+} pg_common_se;
+
+/* poutre::se::Compound_NL_SE, se_types_and_tags.hpp:59-63 */
+typedef enum pg_compound_se { PG_COMPOUND_UNDEF = 0, PG_COMPOUND_OCTAGON = 1, PG_COMPOUND_RHOMBICUBOCTAHEDRON = 2 } pg_compound_se;
+
+/* poutre::geo::reconstruction_type, include/poutre/geodesy/mreconstruct.hpp:28-31 */
+typedef enum pg_reconstruction_type { PG_RECONSTRUCT_ERODE = 0, PG_RECONSTRUCT_DILATE = 1 } pg_reconstruction_type;
+
+/* A device image (the role of poutre::IInterface / image_t<T,Rank> at the boundary). */
+typedef struct pg_image {
+  void *data;       /* device pointer, dense row-major                   */
+  int32_t ptype;    /* pg_ptype                                          */
+  int32_t rank;     /* 1, 2 or 3                                         */
+  int64_t shape[3]; /* d0 .. d_{rank-1}; unused entries ignored          */
+} pg_image;
+
+/* Structuring element for the composite filters (opening/closing/gradient), which the
+ * reference does not have: one of its SE vocabularies, selected by `kind`. */
+typedef enum pg_se_kind {
+  PG_SE_KIND_STATIC = 0,   /* common_se iterated `iter` times (Erode/Dilate(.., Common_NL_SE, iter, ..)) */
+  PG_SE_KIND_RECT = 1,     /* flat (2*hy+1) x (2*hx+1) rectangle = line Y(hy) o line X(hx)              */
+  PG_SE_KIND_LINE = 2,     /* segment t*(dy,dx), t in [-half, half]; (0,1) X, (1,0) Y, (-1,1) 45 degrees */
+  PG_SE_KIND_NL = 3        /* explicit offset list (neighbor_list_t), host array n x rank               */
+} pg_se_kind;
+
+typedef struct pg_se {
+  int32_t kind;
+  int32_t common_se, iter;           /* PG_SE_KIND_STATIC */
+  int32_t hy, hx;                    /* PG_SE_KIND_RECT   */
+  int32_t dy, dx, half;              /* PG_SE_KIND_LINE   */
+  const int32_t *offsets; int32_t n; /* PG_SE_KIND_NL     */
+} pg_se;
+
+PG_API const char *pg_last_error(void);
+PG_API const char *pg_version(void);
+
+/* ---------------------------------------------------------------- low_level_morpho */
+
+/* poutre::Erode / poutre::Dilate(const IInterface&, se::Common_NL_SE, int iter, IInterface&)
+ * include/poutre/low_level_morpho/ero_dil.hpp:32-35 (src/low_level_morpho/ero_dil_static.cpp:229-306) */
+PG_API pg_status pg_erode(const pg_image *in, int32_t common_se, int32_t iter, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate(const pg_image *in, int32_t common_se, int32_t iter, const pg_image *out, pg_stream_t stream);
+
+/* poutre::Erode / Dilate(const IInterface&, se::Compound_NL_SE, int size, IInterface&), ero_dil.hpp:38-41
+ * (ero_dil_compound_static_se_t.hpp:34-160) */
+PG_API pg_status pg_erode_compound(const pg_image *in, int32_t compound_se, int32_t size, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate_compound(const pg_image *in, int32_t compound_se, int32_t size, const pg_image *out, pg_stream_t stream);
+
+/* poutre::Erode / Dilate(const IInterface&, const se::IStructuringElement&, IInterface&), ero_dil.hpp:44-47
+ * with a neighbour list: `offsets` is a HOST array of n offsets of `in->rank` ints each, reference
+ * coordinate order (neighbor_list_t<Rank>, neighbor_list_se_t.hpp:36-228). n <= 4096. */
+PG_API pg_status pg_erode_nl(const pg_image *in, const int32_t *offsets, int32_t n, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate_nl(const pg_image *in, const int32_t *offsets, int32_t n, const pg_image *out, pg_stream_t stream);
+
+/* poutre::ErodeX / DilateX / ErodeY / DilateY(const IInterface&, ptrdiff_t size_half_segment, IInterface&)
+ * include/poutre/low_level_morpho/ero_dil_line.hpp:32-47.  Y requires a square 2D image, as in the reference. */
+PG_API pg_status pg_erode_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_erode_y(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate_y(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t stream);
+
+/* Erosion / dilation / opening / closing / morphological gradient by any pg_se.  No reference
+ * counterpart (low_level_morpho.hpp:15 announces them); opening = dilate(erode(.)), closing =
+ * erode(dilate(.)), gradient = dilate(.) - erode(.) (plain subtraction). */
+PG_API pg_status pg_erode_se(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dilate_se(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_opening(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_closing(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_gradient(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
+
+/* ---------------------------------------------------------------- geodesy */
+
+/* poutre::geo::Reconstruction(reconstruction_type, const IInterface& marker, const IInterface& mask,
+ * se::Common_NL_SE, IInterface&), include/poutre/geodesy/mreconstruct.hpp:37-41.
+ * 1D (SESegmentX1D) and 2D (SESquare2D, SECross2D) SEs; pixel types u8, u16, i32, i64, f32, f64. */
+PG_API pg_status pg_reconstruction(int32_t type, const pg_image *marker, const pg_image *mask, int32_t common_se,
+                            const pg_image *out, pg_stream_t stream);
+
+/* poutre::geo::h_minima / h_maxima / h_concave / h_convex / dynamic_pseudo_opening /
+ * dynamic_pseudo_closing(const IInterface&, const ScalarTypeVariant& h, se::Common_NL_SE, IInterface&),
+ * include/poutre/geodesy/extrema.hpp:33-64.  `h` must be exactly representable in the pixel type
+ * (the reference requires the variant to hold the pixel type, src/pixel_processing/arith.cpp:55). */
+PG_API pg_status pg_h_minima(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_maxima(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_concave(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_convex(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dynamic_pseudo_opening(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dynamic_pseudo_closing(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+
+/* Binary regional maxima of the h-maxima transform, one fused launch: out(u8) = 255 where
+ * in > h_maxima(in) else 0, i.e. h_maxima followed by CompareImage(in, CompOpSup, rec, 255, 0)
+ * (include/poutre/pixel_processing/compare.hpp:69). `out` is a u8 image of in's shape. */
+PG_API pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+
+/* Ragged batch of the binary h-maxima: n independent 2D images of any sizes in ONE persistent
+ * launch (tile table over all images).  ins[i]/outs[i] are device images (outs u8). */
+PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t common_se,
+                                   pg_stream_t stream);
+
+/* poutre::geo::low_leveling / high_leveling / leveling(const IInterface& ref, const IInterface& marker,
+ * se::Common_NL_SE, IInterface&), include/poutre/geodesy/leveling.hpp:37-52. */
+PG_API pg_status pg_low_leveling(const pg_image *ref, const pg_image *marker, int32_t common_se, const pg_image *out,
+                          pg_stream_t stream);
+PG_API pg_status pg_high_leveling(const pg_image *ref, const pg_image *marker, int32_t common_se, const pg_image *out,
+                           pg_stream_t stream);
+PG_API pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_t common_se, const pg_image *out,
+                      pg_stream_t stream);
+
+/* ---------------------------------------------------------------- pixel_processing subset */
+
+/* poutre::ArithSaturatedSubConstant / ArithSaturatedAddConstant (src/pixel_processing/arith.cpp:471),
+ * integer pixel types. */
+PG_API pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
+
+/* ---------------------------------------------------------------- flat morphology adjoint (float32) */
+
+/* Flat dilation (dilate != 0) or erosion by a (2*ry+1) x (2*rx+1) rectangle of `planes` stacked
+ * h x w float32 planes (an NCHW tensor with planes = N*C), and its adjoint: grad_in[q] is the sum,
+ * in raster order of the outputs, of grad_out[p] over every output p whose first-in-scan-order
+ * (dy-major, then dx) arg-extremum within its clipped window is q.  Deterministic (gather, no
+ * atomics).  No reference counterpart.  ry, rx <= 7. */
+PG_API pg_status pg_flat_morph2d_forward(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int32_t ry,
+                                  int32_t rx, int32_t dilate, pg_stream_t stream);
+PG_API pg_status pg_flat_morph2d_backward(const float *x, const float *grad_out, float *grad_in, int64_t planes, int64_t h,
+                                   int64_t w, int32_t ry, int32_t rx, int32_t dilate, pg_stream_t stream);
+
+/* Synchronises `stream`, then returns (and clears) the device-side status of the geodesy
+ * kernels: PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device
+ * wait) since the last check, else PG_OK.  The geodesy calls above are asynchronous; call this
+ * to observe the failure the reference would have thrown. */
+PG_API pg_status pg_check_device(pg_stream_t stream);
+
+/* Number of persistent rounds the last completed reconstruction on the current device needed
+ * (diagnostics; synchronises the device). */
+PG_API int32_t pg_last_reconstruction_rounds(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POUTRE_GB300_H */

@@ -1,0 +1,116 @@
+"""ctypes binding of ``_build/libpoutre_gb300.so`` (the C ABI of ``include/poutre_gb300.h``).
+
+The library is the only compute path.  Loading fails loudly (``PoutreError``) when it has
+not been built or when no CUDA device is present; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libpoutre_gb300.so")
+
+PG_OK = 0
+STATUS_NAMES = {
+    0: "PG_OK", 1: "PG_ERR_INVALID_ARGUMENT", 2: "PG_ERR_UNSUPPORTED_PTYPE", 3: "PG_ERR_UNSUPPORTED_SE",
+    4: "PG_ERR_INCOMPATIBLE", 5: "PG_ERR_ALIASING", 6: "PG_ERR_NOT_SQUARE", 7: "PG_ERR_CUDA",
+    8: "PG_ERR_OUT_OF_MEMORY", 9: "PG_ERR_NOT_CONVERGED",
+}
+
+# every symbol include/poutre_gb300.h declares
+EXPORTED = [
+    "pg_last_error", "pg_version",
+    "pg_erode", "pg_dilate", "pg_erode_compound", "pg_dilate_compound", "pg_erode_nl", "pg_dilate_nl",
+    "pg_erode_x", "pg_dilate_x", "pg_erode_y", "pg_dilate_y",
+    "pg_erode_se", "pg_dilate_se", "pg_opening", "pg_closing", "pg_gradient",
+    "pg_reconstruction", "pg_h_minima", "pg_h_maxima", "pg_h_concave", "pg_h_convex",
+    "pg_dynamic_pseudo_opening", "pg_dynamic_pseudo_closing", "pg_h_maxima_binary", "pg_h_maxima_binary_batch",
+    "pg_low_leveling", "pg_high_leveling", "pg_leveling",
+    "pg_sat_sub_constant", "pg_sat_add_constant",
+    "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
+    "pg_check_device", "pg_last_reconstruction_rounds",
+]
+
+
+class PoutreError(RuntimeError):
+    """Raised where poutre2 throws std::runtime_error (the C ABI returned a non-zero status)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class PgImage(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("ptype", ctypes.c_int32), ("rank", ctypes.c_int32),
+                ("shape", ctypes.c_int64 * 3)]
+
+
+class PgSE(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("common_se", ctypes.c_int32), ("iter", ctypes.c_int32),
+                ("hy", ctypes.c_int32), ("hx", ctypes.c_int32), ("dy", ctypes.c_int32), ("dx", ctypes.c_int32),
+                ("half", ctypes.c_int32), ("offsets", ctypes.POINTER(ctypes.c_int32)), ("n", ctypes.c_int32)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the library (once).  Raises PoutreError if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise PoutreError(7, f"CUDA library not built: {p} (run __graft_entry__.build())")
+        L = ctypes.CDLL(p)
+        img = ctypes.POINTER(PgImage)
+        se = ctypes.POINTER(PgSE)
+        I32, I64, D, VP = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        fp = ctypes.c_void_p
+        sig = {
+            "pg_erode": [img, I32, I32, img, VP], "pg_dilate": [img, I32, I32, img, VP],
+            "pg_erode_compound": [img, I32, I32, img, VP], "pg_dilate_compound": [img, I32, I32, img, VP],
+            "pg_erode_nl": [img, i32p, I32, img, VP], "pg_dilate_nl": [img, i32p, I32, img, VP],
+            "pg_erode_x": [img, I64, img, VP], "pg_dilate_x": [img, I64, img, VP],
+            "pg_erode_y": [img, I64, img, VP], "pg_dilate_y": [img, I64, img, VP],
+            "pg_erode_se": [img, se, img, VP], "pg_dilate_se": [img, se, img, VP],
+            "pg_opening": [img, se, img, VP], "pg_closing": [img, se, img, VP], "pg_gradient": [img, se, img, VP],
+            "pg_reconstruction": [I32, img, img, I32, img, VP],
+            "pg_h_minima": [img, D, I32, img, VP], "pg_h_maxima": [img, D, I32, img, VP],
+            "pg_h_concave": [img, D, I32, img, VP], "pg_h_convex": [img, D, I32, img, VP],
+            "pg_dynamic_pseudo_opening": [img, D, I32, img, VP], "pg_dynamic_pseudo_closing": [img, D, I32, img, VP],
+            "pg_h_maxima_binary": [img, D, I32, img, VP],
+            "pg_h_maxima_binary_batch": [img, img, I32, D, I32, VP],
+            "pg_low_leveling": [img, img, I32, img, VP], "pg_high_leveling": [img, img, I32, img, VP],
+            "pg_leveling": [img, img, I32, img, VP],
+            "pg_sat_sub_constant": [img, D, img, VP], "pg_sat_add_constant": [img, D, img, VP],
+            "pg_flat_morph2d_forward": [fp, fp, I64, I64, I64, I32, I32, I32, VP],
+            "pg_flat_morph2d_backward": [fp, fp, fp, I64, I64, I64, I32, I32, I32, VP],
+            "pg_check_device": [VP],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = ctypes.c_int
+        L.pg_last_error.restype = ctypes.c_char_p
+        L.pg_last_error.argtypes = []
+        L.pg_version.restype = ctypes.c_char_p
+        L.pg_version.argtypes = []
+        L.pg_last_reconstruction_rounds.restype = ctypes.c_int32
+        L.pg_last_reconstruction_rounds.argtypes = []
+        _lib = L
+        return L
+
+
+def check(status: int):
+    if status != PG_OK:
+        raise PoutreError(status, load().pg_last_error().decode(errors="replace"))
+
+
+def call(name: str, *args):
+    check(getattr(load(), name)(*args))

@@ -1,0 +1,489 @@
+// capi.cu -- the extern "C" boundary: argument checks that mirror the reference's
+// (AssertSizesCompatible / AssertAsTypesCompatible / AssertImagesAreDifferent, the
+// rank x PType x SE switches of src/low_level_morpho/*.cpp and src/geodesy/*.cpp), then
+// dispatch to the kernels.  No exception crosses the boundary.
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pg {
+
+static thread_local std::string t_err;
+
+void set_error(const std::string &msg) { t_err = msg; }
+
+pg_status fail(pg_status st, const std::string &msg) {
+  t_err = msg;
+  return st;
+}
+
+pg_status cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return PG_OK;
+  t_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? PG_ERR_OUT_OF_MEMORY : PG_ERR_CUDA;
+}
+
+int num_sms() {
+  static std::mutex mu;
+  static int cached_dev = -1, cached = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev != cached_dev) {
+    if (cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) cached = 1;
+    cached_dev = dev;
+  }
+  return cached;
+}
+
+// ------------------------------------------------------------------ checks
+static pg_status check_image(const pg_image *im, const char *what) {
+  if (!im) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": null image descriptor");
+  if (im->rank < 1 || im->rank > 3) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": unsupported number of dims");
+  if (!elem_size(im->ptype)) return fail(PG_ERR_UNSUPPORTED_PTYPE, std::string(what) + ": unsupported PTYPE");
+  int64_t n = 1;
+  for (int i = 0; i < im->rank; ++i) {
+    if (im->shape[i] < 0) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": negative dimension");
+    n *= im->shape[i];
+  }
+  if (n > 0 && !im->data) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": null data pointer");
+  return PG_OK;
+}
+
+static bool same_geometry(const pg_image &a, const pg_image &b) {
+  if (a.rank != b.rank) return false;
+  for (int i = 0; i < a.rank; ++i) if (a.shape[i] != b.shape[i]) return false;
+  return true;
+}
+
+static bool overlaps(const pg_image &a, const pg_image &b) {
+  const size_t na = (size_t)dims_of(a).count() * elem_size(a.ptype), nb = (size_t)dims_of(b).count() * elem_size(b.ptype);
+  if (na == 0 || nb == 0) return false;
+  const char *pa = static_cast<const char *>(a.data), *pb = static_cast<const char *>(b.data);
+  return pa < pb + nb && pb < pa + na;
+}
+
+// in -> out of the same geometry and type, distinct buffers
+static pg_status check_in_out(const pg_image *in, const pg_image *out, const char *what) {
+  PG_TRY(check_image(in, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images have not compatible sizes");
+  if (in->ptype != out->ptype) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images must have compatible types");
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, std::string(what) + " input output images must be different");
+  return PG_OK;
+}
+
+static int se_rank(int se) {
+  switch (se) {
+    case PG_SE_SEGMENT_X_1D: return 1;
+    case PG_SE_SQUARE_2D: case PG_SE_CROSS_2D: case PG_SE_SEGMENT_X_2D: case PG_SE_SEGMENT_Y_2D: return 2;
+    case PG_SE_SEGMENT_X_3D: case PG_SE_SEGMENT_Y_3D: case PG_SE_SEGMENT_Z_3D: case PG_SE_CROSS_3D: case PG_SE_SQUARE_3D: return 3;
+    default: return 0;
+  }
+}
+
+// integer pixel scalar must be an exact value of the pixel type (ScalarTypeVariant holds
+// exactly the image's type, src/pixel_processing/arith.cpp:55)
+static pg_status check_scalar(int ptype, double v, const char *what) {
+  if (!std::isfinite(v)) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": non-finite scalar");
+  double lo = 0, hi = 0;
+  switch (ptype) {
+    case PG_PTYPE_U8: lo = 0; hi = 255; break;
+    case PG_PTYPE_U16: lo = 0; hi = 65535; break;
+    case PG_PTYPE_I32: lo = -2147483648.0; hi = 2147483647.0; break;
+    case PG_PTYPE_I64: lo = -9223372036854775808.0; hi = 9223372036854774784.0; break;
+    default: return PG_OK;
+  }
+  if (v != std::floor(v) || v < lo || v > hi)
+    return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": scalar is not a value of the pixel type");
+  return PG_OK;
+}
+
+// ------------------------------------------------------------------ erosion / dilation
+static pg_status static_iter(const pg_image &in, int se, int iter, const pg_image &out, bool dilate, cudaStream_t s) {
+  if (se_rank(se) == 0 || se_rank(se) != in.rank) return fail(PG_ERR_UNSUPPORTED_SE, "unsupported nl_static");
+  if (iter < 0) return fail(PG_ERR_INVALID_ARGUMENT, "iter must be >= 0");
+  if (iter == 0) return launch_copy(in, out, s);
+  if (iter == 1) return launch_small_se(in, out, se, dilate, s);
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
+  pg_image t = in;
+  t.data = tmp.ptr;
+  // pass k writes `out` when (iter - k) is even, so the last pass lands in `out`
+  const pg_image *src = &in;
+  for (int k = 1; k <= iter; ++k) {
+    const pg_image *dst = ((iter - k) % 2 == 0) ? &out : &t;
+    PG_TRY(launch_small_se(*src, *dst, se, dilate, s));
+    src = dst;
+  }
+  return PG_OK;
+}
+
+// sequence of static passes (compound SEs): passes[i] applied in order
+static pg_status static_sequence(const pg_image &in, const std::vector<int> &passes, const pg_image &out, bool dilate,
+                                 cudaStream_t s) {
+  const int n = (int)passes.size();
+  if (n == 0) return launch_copy(in, out, s);
+  if (n == 1) return launch_small_se(in, out, passes[0], dilate, s);
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
+  pg_image t = in;
+  t.data = tmp.ptr;
+  const pg_image *src = &in;
+  for (int k = 1; k <= n; ++k) {
+    const pg_image *dst = ((n - k) % 2 == 0) ? &out : &t;
+    PG_TRY(launch_small_se(*src, *dst, passes[k - 1], dilate, s));
+    src = dst;
+  }
+  return PG_OK;
+}
+
+// t_DilateOctagon / t_DilateRhombicuboctahedron (ero_dil_compound_static_se_t.hpp:34-160):
+// `size` passes, the last round(size / (1 + sqrt 2)) of them by the square, the others by
+// the cross.
+static pg_status compound(const pg_image &in, int compound_se, int size, const pg_image &out, bool dilate, cudaStream_t s) {
+  int cross, square;
+  if (compound_se == PG_COMPOUND_OCTAGON) {
+    if (in.rank != 2) return fail(PG_ERR_INVALID_ARGUMENT, "Octagon: unsupported number of dims");
+    cross = PG_SE_CROSS_2D; square = PG_SE_SQUARE_2D;
+  } else if (compound_se == PG_COMPOUND_RHOMBICUBOCTAHEDRON) {
+    if (in.rank != 3) return fail(PG_ERR_INVALID_ARGUMENT, "Rhombicuboctahedron: unsupported number of dims");
+    // size 1 applies the 2D cross to the volume in the reference, which t_Dilate rejects
+    if (size == 1) return fail(PG_ERR_UNSUPPORTED_SE, "unsupported nl_static");
+    cross = PG_SE_CROSS_3D; square = PG_SE_SQUARE_3D;
+  } else {
+    return fail(PG_ERR_UNSUPPORTED_SE, "unsupported Compound_NL_SE");
+  }
+  if (size < 0) return fail(PG_ERR_INVALID_ARGUMENT, "size must be >= 0");
+  if (size == 0) return launch_copy(in, out, s);
+  if (size == 1) return launch_small_se(in, out, cross, dilate, s);
+  const double nb = (double)size / (1.0 + std::sqrt(2.0));
+  const double fl = std::floor(nb);
+  const int nb_square = (int)((nb - fl) < 0.5 ? fl : fl + 1);
+  std::vector<int> passes;
+  passes.push_back(cross);
+  for (int i = 1; i < size - nb_square; ++i) passes.push_back(cross);
+  for (int i = 0; i < nb_square; ++i) passes.push_back(square);
+  return static_sequence(in, passes, out, dilate, s);
+}
+
+static pg_status by_se(const pg_image &in, const pg_se &se, const pg_image &out, bool dilate, cudaStream_t s) {
+  switch (se.kind) {
+    case PG_SE_KIND_STATIC: return static_iter(in, se.common_se, se.iter, out, dilate, s);
+    case PG_SE_KIND_RECT:
+      if (in.rank != 2) return fail(PG_ERR_UNSUPPORTED_SE, "rectangle SE needs a 2D image");
+      return launch_rect(in, out, se.hy, se.hx, dilate, s);
+    case PG_SE_KIND_LINE:
+      if (in.rank != 2) return fail(PG_ERR_UNSUPPORTED_SE, "line SE needs a 2D image");
+      if (se.half < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative half segment");
+      return launch_line(in, out, se.dy, se.dx, se.half, dilate, s);
+    case PG_SE_KIND_NL:
+      if (!se.offsets || se.n < 1 || se.n > 4096) return fail(PG_ERR_INVALID_ARGUMENT, "neighbour list must hold 1..4096 offsets");
+      return launch_nl(in, out, se.offsets, se.n, dilate, s);
+    default: return fail(PG_ERR_UNSUPPORTED_SE, "unknown pg_se kind");
+  }
+}
+
+enum Composite { C_OPEN, C_CLOSE, C_GRAD };
+static pg_status composite(const pg_image &in, const pg_se &se, const pg_image &out, Composite c, cudaStream_t s) {
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
+  pg_image t = in;
+  t.data = tmp.ptr;
+  if (c == C_OPEN) {
+    PG_TRY(by_se(in, se, t, false, s));
+    return by_se(t, se, out, true, s);
+  }
+  if (c == C_CLOSE) {
+    PG_TRY(by_se(in, se, t, true, s));
+    return by_se(t, se, out, false, s);
+  }
+  Scratch tmp2;
+  PG_TRY(tmp2.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
+  pg_image e = in;
+  e.data = tmp2.ptr;
+  PG_TRY(by_se(in, se, t, true, s));
+  PG_TRY(by_se(in, se, e, false, s));
+  return launch_sub(t, e, out, s);
+}
+
+// ------------------------------------------------------------------ geodesy helpers
+static pg_status recon_se(int se, int rank, bool &conn8) {
+  if (rank == 1 && se == PG_SE_SEGMENT_X_1D) { conn8 = true; return PG_OK; }
+  if (rank == 2 && se == PG_SE_SQUARE_2D) { conn8 = true; return PG_OK; }
+  if (rank == 2 && se == PG_SE_CROSS_2D) { conn8 = false; return PG_OK; }
+  if (rank == 3 && (se == PG_SE_CROSS_3D || se == PG_SE_SQUARE_3D))
+    return fail(PG_ERR_UNSUPPORTED_SE, "3D reconstruction is not available on the GPU path");
+  return fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
+}
+
+static pg_status h_recon(const pg_image *in, double h, int se, const pg_image *out, bool maxima, cudaStream_t s) {
+  ReconRequest rq;
+  PG_TRY(recon_se(se, in->rank, rq.conn8));
+  rq.dilate = maxima;
+  rq.init = INIT_SAT_CONST;
+  rq.h = h;
+  return launch_reconstruction(nullptr, in, out, 1, rq, s);
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+#define STREAM(s) reinterpret_cast<cudaStream_t>(s)
+
+extern "C" {
+
+const char *pg_last_error(void) { return t_err.c_str(); }
+const char *pg_version(void) { return "poutre2_gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- low_level_morpho
+pg_status pg_erode(const pg_image *in, int32_t se, int32_t iter, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Erode iter"));
+  return static_iter(*in, se, iter, *out, false, STREAM(s));
+}
+pg_status pg_dilate(const pg_image *in, int32_t se, int32_t iter, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Dilate iter"));
+  return static_iter(*in, se, iter, *out, true, STREAM(s));
+}
+pg_status pg_erode_compound(const pg_image *in, int32_t cse, int32_t size, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Erode compound"));
+  return compound(*in, cse, size, *out, false, STREAM(s));
+}
+pg_status pg_dilate_compound(const pg_image *in, int32_t cse, int32_t size, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Dilate compound"));
+  return compound(*in, cse, size, *out, true, STREAM(s));
+}
+pg_status pg_erode_nl(const pg_image *in, const int32_t *offsets, int32_t n, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Erode IStructuringElement"));
+  if (!offsets || n < 1 || n > 4096) return fail(PG_ERR_INVALID_ARGUMENT, "neighbour list must hold 1..4096 offsets");
+  return launch_nl(*in, *out, offsets, n, false, STREAM(s));
+}
+pg_status pg_dilate_nl(const pg_image *in, const int32_t *offsets, int32_t n, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Dilate IStructuringElement"));
+  if (!offsets || n < 1 || n > 4096) return fail(PG_ERR_INVALID_ARGUMENT, "neighbour list must hold 1..4096 offsets");
+  return launch_nl(*in, *out, offsets, n, true, STREAM(s));
+}
+
+static pg_status line_x(const pg_image *in, int64_t half, const pg_image *out, bool dilate, cudaStream_t s,
+                        const char *what) {
+  PG_TRY(check_in_out(in, out, what));
+  if (in->rank > 2) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + " Unsupported number of dims");
+  if (half <= 0) return launch_copy(*in, *out, s);  // size_line_segment <= 0 copies (ero_dil_line_se_t.hpp:161-164)
+  return launch_line(*in, *out, 0, 1, half, dilate, s);
+}
+static pg_status line_y(const pg_image *in, int64_t half, const pg_image *out, bool dilate, cudaStream_t s,
+                        const char *what) {
+  PG_TRY(check_in_out(in, out, what));
+  if (in->rank != 2) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + " Unsupported number of dims");
+  // t_DilateY transposes into a temporary of the input's shape (ero_dil_line_se_t.hpp:258)
+  if (in->shape[0] != in->shape[1]) return fail(PG_ERR_NOT_SQUARE, std::string(what) + " needs a square image (t_transpose)");
+  if (half <= 0) return launch_copy(*in, *out, s);
+  return launch_line(*in, *out, 1, 0, half, dilate, s);
+}
+pg_status pg_erode_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_x(in, half, out, false, STREAM(s), "ErodeX"); }
+pg_status pg_dilate_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_x(in, half, out, true, STREAM(s), "DilateX"); }
+pg_status pg_erode_y(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_y(in, half, out, false, STREAM(s), "ErodeY"); }
+pg_status pg_dilate_y(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_y(in, half, out, true, STREAM(s), "DilateY"); }
+
+pg_status pg_erode_se(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Erode"));
+  if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
+  return by_se(*in, *se, *out, false, STREAM(s));
+}
+pg_status pg_dilate_se(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Dilate"));
+  if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
+  return by_se(*in, *se, *out, true, STREAM(s));
+}
+pg_status pg_opening(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Opening"));
+  if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
+  return composite(*in, *se, *out, C_OPEN, STREAM(s));
+}
+pg_status pg_closing(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Closing"));
+  if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
+  return composite(*in, *se, *out, C_CLOSE, STREAM(s));
+}
+pg_status pg_gradient(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "Gradient"));
+  if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
+  return composite(*in, *se, *out, C_GRAD, STREAM(s));
+}
+
+// ---------------------------------------------------------------- geodesy
+pg_status pg_reconstruction(int32_t type, const pg_image *marker, const pg_image *mask, int32_t se, const pg_image *out,
+                            pg_stream_t s) {
+  PG_TRY(check_in_out(marker, out, "t_Reconstruct"));
+  PG_TRY(check_in_out(mask, out, "t_Reconstruct"));
+  if (type != PG_RECONSTRUCT_ERODE && type != PG_RECONSTRUCT_DILATE)
+    return fail(PG_ERR_INVALID_ARGUMENT, "t_ReconstructionDispatchRectType unsupported reconstruction_type");
+  ReconRequest rq;
+  PG_TRY(recon_se(se, mask->rank, rq.conn8));
+  rq.dilate = type == PG_RECONSTRUCT_DILATE;
+  return launch_reconstruction(marker, mask, out, 1, rq, STREAM(s));
+}
+
+pg_status pg_h_maxima(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "h_maxima"));
+  PG_TRY(check_scalar(in->ptype, h, "h_maxima"));
+  return h_recon(in, h, se, out, true, STREAM(s));
+}
+pg_status pg_h_minima(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "h_minima"));
+  PG_TRY(check_scalar(in->ptype, h, "h_minima"));
+  return h_recon(in, h, se, out, false, STREAM(s));
+}
+pg_status pg_h_convex(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "h_convex"));
+  PG_TRY(check_scalar(in->ptype, h, "h_convex"));
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(*in).count() * elem_size(in->ptype), STREAM(s)));
+  pg_image t = *in;
+  t.data = tmp.ptr;
+  PG_TRY(h_recon(in, h, se, &t, true, STREAM(s)));
+  return launch_sat_sub_image(*in, t, *out, STREAM(s));  // sat_sub(f, h_maxima(f)) (extrema.cpp:63-73)
+}
+pg_status pg_h_concave(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "h_concave"));
+  PG_TRY(check_scalar(in->ptype, h, "h_concave"));
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(*in).count() * elem_size(in->ptype), STREAM(s)));
+  pg_image t = *in;
+  t.data = tmp.ptr;
+  PG_TRY(h_recon(in, h, se, &t, false, STREAM(s)));
+  return launch_sat_sub_image(t, *in, *out, STREAM(s));  // sat_sub(h_minima(f), f) (extrema.cpp:51-61)
+}
+
+static pg_status dyn_pseudo(const pg_image *in, double h, int se, const pg_image *out, bool opening, cudaStream_t s) {
+  Scratch a, b;
+  const size_t bytes = (size_t)dims_of(*in).count() * elem_size(in->ptype);
+  PG_TRY(a.alloc(bytes, s));
+  PG_TRY(b.alloc(bytes, s));
+  pg_image ext = *in, mk = *in;
+  ext.data = a.ptr;
+  mk.data = b.ptr;
+  PG_TRY(h_recon(in, h, se, &ext, opening, s));
+  PG_TRY(launch_dyn_pseudo_marker(*in, ext, h, opening, mk, s));
+  ReconRequest rq;
+  PG_TRY(recon_se(se, in->rank, rq.conn8));
+  rq.dilate = opening;
+  return launch_reconstruction(&mk, in, out, 1, rq, s);
+}
+pg_status pg_dynamic_pseudo_opening(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "dynamic_pseudo_opening"));
+  PG_TRY(check_scalar(in->ptype, h, "dynamic_pseudo_opening"));
+  return dyn_pseudo(in, h, se, out, true, STREAM(s));
+}
+pg_status pg_dynamic_pseudo_closing(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "dynamic_pseudo_closing"));
+  PG_TRY(check_scalar(in->ptype, h, "dynamic_pseudo_closing"));
+  return dyn_pseudo(in, h, se, out, false, STREAM(s));
+}
+
+static pg_status check_binary_out(const pg_image *in, const pg_image *out, const char *what) {
+  PG_TRY(check_image(in, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images have not compatible sizes");
+  if (out->ptype != PG_PTYPE_U8) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " output must be uint8");
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, std::string(what) + " input output images must be different");
+  return PG_OK;
+}
+
+pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_binary_out(in, out, "h_maxima_binary"));
+  PG_TRY(check_scalar(in->ptype, h, "h_maxima_binary"));
+  ReconRequest rq;
+  PG_TRY(recon_se(se, in->rank, rq.conn8));
+  rq.dilate = true;
+  rq.init = INIT_SAT_CONST;
+  rq.epi = EPI_BINARY_SUP;
+  rq.h = h;
+  return launch_reconstruction(nullptr, in, out, 1, rq, STREAM(s));
+}
+
+pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t se,
+                                   pg_stream_t s) {
+  if (n < 0 || (n > 0 && (!ins || !outs))) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch: bad image arrays");
+  if (n == 0) return PG_OK;
+  for (int i = 0; i < n; ++i) {
+    PG_TRY(check_binary_out(&ins[i], &outs[i], "h_maxima_binary_batch"));
+    if (ins[i].ptype != ins[0].ptype || ins[i].rank != ins[0].rank)
+      return fail(PG_ERR_INCOMPATIBLE, "h_maxima_binary_batch: all images must share pixel type and rank");
+  }
+  PG_TRY(check_scalar(ins[0].ptype, h, "h_maxima_binary_batch"));
+  ReconRequest rq;
+  PG_TRY(recon_se(se, ins[0].rank, rq.conn8));
+  rq.dilate = true;
+  rq.init = INIT_SAT_CONST;
+  rq.epi = EPI_BINARY_SUP;
+  rq.h = h;
+  return launch_reconstruction(nullptr, ins, outs, n, rq, STREAM(s));
+}
+
+static pg_status leveling_half(const pg_image *ref, const pg_image *marker, int se, const pg_image *out, bool low,
+                               cudaStream_t s) {
+  ReconRequest rq;
+  PG_TRY(recon_se(se, ref->rank, rq.conn8));
+  rq.dilate = low;
+  rq.init = INIT_MARKER;
+  rq.mask_mode = low ? MASK_MAX_MARKER : MASK_MIN_MARKER;
+  rq.epi = EPI_CLIP_REF;
+  return launch_reconstruction(marker, ref, out, 1, rq, s);
+}
+static pg_status check_leveling(const pg_image *ref, const pg_image *marker, const pg_image *out, const char *what) {
+  PG_TRY(check_in_out(ref, out, what));
+  PG_TRY(check_in_out(marker, out, what));
+  return PG_OK;
+}
+pg_status pg_low_leveling(const pg_image *ref, const pg_image *marker, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_leveling(ref, marker, out, "low_leveling"));
+  return leveling_half(ref, marker, se, out, true, STREAM(s));
+}
+pg_status pg_high_leveling(const pg_image *ref, const pg_image *marker, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_leveling(ref, marker, out, "high_leveling"));
+  return leveling_half(ref, marker, se, out, false, STREAM(s));
+}
+pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_t se, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_leveling(ref, marker, out, "leveling"));
+  Scratch tmp;
+  PG_TRY(tmp.alloc((size_t)dims_of(*ref).count() * elem_size(ref->ptype), STREAM(s)));
+  pg_image t = *ref;
+  t.data = tmp.ptr;
+  PG_TRY(leveling_half(ref, marker, se, &t, false, STREAM(s)));  // high_leveling(ref, marker)
+  return leveling_half(&t, marker, se, out, true, STREAM(s));     // low_leveling(that, marker)
+}
+
+// ---------------------------------------------------------------- pixel processing
+pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "ArithSaturatedSubConstant"));
+  PG_TRY(check_scalar(in->ptype, v, "ArithSaturatedSubConstant"));
+  return launch_sat_const(*in, v, false, *out, STREAM(s));
+}
+pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_in_out(in, out, "ArithSaturatedAddConstant"));
+  PG_TRY(check_scalar(in->ptype, v, "ArithSaturatedAddConstant"));
+  return launch_sat_const(*in, v, true, *out, STREAM(s));
+}
+
+// ---------------------------------------------------------------- adjoint
+pg_status pg_flat_morph2d_forward(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int32_t ry,
+                                  int32_t rx, int32_t dilate, pg_stream_t s) {
+  if (planes < 0 || h < 0 || w < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative dimension");
+  if (planes * h * w > 0 && (!x || !y)) return fail(PG_ERR_INVALID_ARGUMENT, "null tensor");
+  if (x == y && x) return fail(PG_ERR_ALIASING, "input output tensors must be different");
+  return launch_flat2d(x, y, planes, h, w, ry, rx, dilate != 0, STREAM(s));
+}
+pg_status pg_flat_morph2d_backward(const float *x, const float *gy, float *gx, int64_t planes, int64_t h, int64_t w,
+                                   int32_t ry, int32_t rx, int32_t dilate, pg_stream_t s) {
+  if (planes < 0 || h < 0 || w < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative dimension");
+  if (planes * h * w > 0 && (!x || !gy || !gx)) return fail(PG_ERR_INVALID_ARGUMENT, "null tensor");
+  if (gx && (gx == x || gx == gy)) return fail(PG_ERR_ALIASING, "grad_in must be a distinct tensor");
+  return launch_flat2d_backward(x, gy, gx, planes, h, w, ry, rx, dilate != 0, STREAM(s));
+}
+
+}  // extern "C"

@@ -1,0 +1,534 @@
+// recon.cu -- geodesic reconstruction (by dilation / erosion) as one persistent kernel, and
+// the filters built on it: h-extrema (marker made on the fly), low/high leveling (mask and
+// final clip made on the fly), binary h-maxima (comparison fused), ragged batches.
+//
+// Reference: t_ReconstructionViewDispatcher (geodesy/details/mreconstruct_t.hpp:84-195), a
+// sequential Vincent hybrid (raster scan, anti-raster scan, FIFO).  Its result is the
+// least fixpoint rec = min(mask, dilate(rec)) above min(marker, mask) (dual for erosion),
+// which is unique, so any order of monotone updates reaches the same image: the parallel
+// scheme below is bit-exact with it.  Leveling (leveling_t.hpp:45-202) is the same fixpoint
+// with mask max(marker, ref) (low) / min(marker, ref) (high) followed by a clip by ref.
+//
+// GPU design
+//  * The image is cut into 64x64 tiles.  A CTA (64 threads) stages a tile of the current
+//    reconstruction plus a one-pixel halo, and the tile's mask, in shared memory and iterates
+//    directional sweeps there -- down, up (thread per column), right, left (thread per row),
+//    each propagating along its whole direction in one pass -- until a full sweep set
+//    changes nothing: a tile-local fixpoint.  It writes the tile back and flags the
+//    neighbouring tiles whose shared border changed.
+//  * A persistent cooperative grid (all CTAs resident) runs rounds over the flagged tiles
+//    (round 0: all tiles, marker computed from the inputs), separated by a grid barrier,
+//    until a round flags nothing.  Flags live in a double-buffered device worklist; the
+//    "any flag" word is triple-buffered so no CTA resets a word another may still read.
+//  * Reads of other tiles' pixels bypass L1 (ld.global.cg): values only grow (shrink for
+//    erosion), so a concurrently updated halo value is either the old or the new one, both
+//    below the fixpoint; a tile that saw an old value is re-flagged by its writer.
+//  * Every wait is bounded: the grid barrier gives up after kBarrierTimeoutNs and the round
+//    loop after max_rounds, recording PG_ERR_NOT_CONVERGED in a device status word.
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pg {
+
+// tile side = threads per CTA: 64 (32 for 8-byte pixels, to keep the staged tile within the
+// 48 KB static shared-memory limit)
+template <typename T> __host__ __device__ constexpr int tile_side() { return sizeof(T) == 8 ? 32 : 64; }
+static constexpr int kMaxSweeps = 512;
+static constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;  // 4 s
+
+// Device-wide sticky status of the reconstruction kernels (0 = ok) and the round count of
+// the last completed launch.
+__device__ int g_recon_status = 0;
+__device__ int g_recon_rounds = 0;
+
+struct RImg {
+  const void *marker;  // marker (INIT_MARKER and the leveling masks)
+  const void *mask;    // mask, or the leveling reference
+  void *rec;           // reconstruction buffer
+  void *out;           // epilogue output (binary u8 image, or == rec)
+  int64_t H, W;
+  int tiles_x, tiles_y;
+  int tile_begin;
+  int pad;
+};
+
+struct RCtl {
+  unsigned any[3];
+  unsigned bar_count;
+  unsigned bar_gen;
+  int status;
+  int rounds;
+  int pad;
+};
+
+template <typename T> struct RParams {
+  RImg single;        // used when nimg == 1
+  const RImg *imgs;   // device table when nimg > 1
+  int nimg;
+  int ntiles;
+  RCtl *ctl;
+  unsigned *flags;    // 2 * ntiles
+  int max_rounds;
+  int init, mask_mode, epi;
+  T h;
+};
+
+// row pitch (in pixels) of a shared tile: a row spans an odd number of 32-bit words so that
+// thread-per-row sweeps touch 32 distinct banks
+template <typename T> __host__ __device__ constexpr int tile_pitch(int cols) {
+  if constexpr (sizeof(T) <= 4) {
+    int words = (cols * (int)sizeof(T) + 3) / 4;
+    if (words % 2 == 0) ++words;
+    return words * 4 / (int)sizeof(T);
+  } else {
+    return cols | 1;
+  }
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void set_status(RCtl *ctl, int code) {
+  atomicCAS(&ctl->status, 0, code);
+  atomicCAS(&g_recon_status, 0, code);
+}
+
+// Grid barrier with a bounded wait.  Returns false once any CTA recorded an error.
+__device__ bool grid_barrier(RCtl *ctl) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *genp = &ctl->bar_gen;
+    const unsigned gen = *genp;
+    __threadfence();
+    const unsigned arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      atomicExch(&ctl->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&ctl->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      unsigned ns = 32;
+      while (*genp == gen) {
+        __nanosleep(ns);
+        if (ns < 1024) ns <<= 1;
+        if (global_ns() - t0 > kBarrierTimeoutNs) {
+          set_status(ctl, PG_ERR_NOT_CONVERGED);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile int *)&ctl->status) == 0;
+}
+
+template <typename T, bool SUP>
+__device__ __forceinline__ T sat_shift(T m, T h) {
+  // marker of h-maxima (sat_sub) / h-minima (sat_add), op_Saturated_{Sub,Add}_Constant
+  // (pixel_processing/details/arith_op_t.hpp:218-345), clamped to the pixel type's range
+  if constexpr (std::is_integral_v<T>) {
+    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
+    const Wide r = SUP ? (Wide)m - (Wide)h : (Wide)m + (Wide)h;
+    if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
+    if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
+    return (T)r;
+  } else {
+    return SUP ? m - h : m + h;
+  }
+}
+
+// effective mask and initial value of pixel i
+template <typename T, bool SUP>
+__device__ __forceinline__ void pixel_init(const RImg &im, const RParams<T> &P, int64_t i, T &mask, T &init) {
+  const T a = ldg(static_cast<const T *>(im.mask) + i);
+  if (P.init == INIT_SAT_CONST) {
+    mask = a;
+    init = sat_shift<T, SUP>(a, P.h);
+    return;
+  }
+  const T mk = ldg(static_cast<const T *>(im.marker) + i);
+  if (P.mask_mode == MASK_MAX_MARKER) mask = Op<T, true>::apply(mk, a);
+  else if (P.mask_mode == MASK_MIN_MARKER) mask = Op<T, false>::apply(mk, a);
+  else mask = a;
+  init = Op<T, !SUP>::apply(mk, mask);  // select_marker: min(marker, mask) / max for erosion
+}
+
+template <typename T, bool SUP>
+__device__ __forceinline__ T pixel_mask(const RImg &im, const RParams<T> &P, int64_t i) {
+  const T a = ldg(static_cast<const T *>(im.mask) + i);
+  if (P.init == INIT_SAT_CONST || P.mask_mode == MASK_PLAIN) return a;
+  const T mk = ldg(static_cast<const T *>(im.marker) + i);
+  return P.mask_mode == MASK_MAX_MARKER ? Op<T, true>::apply(mk, a) : Op<T, false>::apply(mk, a);
+}
+
+template <typename T> __device__ __forceinline__ T ld_cg(const T *p) {
+  if constexpr (sizeof(T) == 1) return (T)__ldcg(reinterpret_cast<const unsigned char *>(p));
+  else if constexpr (sizeof(T) == 2) return (T)__ldcg(reinterpret_cast<const unsigned short *>(p));
+  else if constexpr (std::is_same_v<T, int64_t>) return (T)__ldcg(reinterpret_cast<const long long *>(p));
+  else return __ldcg(p);
+}
+template <typename T> __device__ __forceinline__ void st_cg(T *p, T v) {
+  if constexpr (sizeof(T) == 1) __stcg(reinterpret_cast<unsigned char *>(p), (unsigned char)v);
+  else if constexpr (sizeof(T) == 2) __stcg(reinterpret_cast<unsigned short *>(p), (unsigned short)v);
+  else if constexpr (std::is_same_v<T, int64_t>) __stcg(reinterpret_cast<long long *>(p), (long long)v);
+  else __stcg(p, v);
+}
+
+enum : int { B_N = 1, B_S = 2, B_W = 4, B_E = 8, B_NW = 16, B_NE = 32, B_SW = 64, B_SE = 128, B_SELF = 256 };
+
+template <typename T, bool SUP, bool CONN8>
+__device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, int round, T *s_out, T *s_mask,
+                             int *s_flag) {
+  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  constexpr int PO = tile_pitch<T>(RT + 2);
+  constexpr int PM = tile_pitch<T>(RT);
+  const T NEU = Op<T, SUP>::neutral();
+  const int tx = t_local % im.tiles_x, ty = t_local / im.tiles_x;
+  const int64_t y0 = (int64_t)ty * RT, x0 = (int64_t)tx * RT;
+  const T *rec_in = static_cast<const T *>(im.rec);
+
+  // stage: current reconstruction (round 0: marker) with halo, effective mask
+  for (int i = threadIdx.x; i < (RT + 2) * (RT + 2); i += RTHREADS) {
+    const int r = i / (RT + 2) - 1, c = i % (RT + 2) - 1;
+    const int64_t gy = y0 + r, gx = x0 + c;
+    const bool inside = gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
+    const bool interior = r >= 0 && r < RT && c >= 0 && c < RT;
+    T v = NEU, m = NEU;
+    if (inside) {
+      const int64_t gi = gy * im.W + gx;
+      if (round == 0) pixel_init<T, SUP>(im, P, gi, m, v);
+      else {
+        v = ld_cg(rec_in + gi);
+        if (interior) m = pixel_mask<T, SUP>(im, P, gi);
+      }
+    }
+    s_out[(r + 1) * PO + (c + 1)] = v;
+    if (interior) s_mask[r * PM + c] = m;
+  }
+  if (threadIdx.x == 0) *s_flag = 0;
+  __syncthreads();
+
+  int bflags = 0;
+  bool converged = false;
+  // one update: v = sel(op(cur, nb), mask); values are monotone, so "changed" means "grew"
+  auto upd = [&](int r, int c, T nb) -> bool {
+    T *cell = s_out + (r + 1) * PO + (c + 1);
+    const T cur = *cell;
+    const T v = Op<T, !SUP>::apply(Op<T, SUP>::apply(cur, nb), s_mask[r * PM + c]);
+    if (v != cur) {
+      *cell = v;
+      if (r == 0) bflags |= B_N;
+      if (r == RT - 1) bflags |= B_S;
+      if (c == 0) bflags |= B_W;
+      if (c == RT - 1) bflags |= B_E;
+      if (r == 0 && c == 0) bflags |= B_NW;
+      if (r == 0 && c == RT - 1) bflags |= B_NE;
+      if (r == RT - 1 && c == 0) bflags |= B_SW;
+      if (r == RT - 1 && c == RT - 1) bflags |= B_SE;
+      return true;
+    }
+    return false;
+  };
+  const int lane = threadIdx.x;  // column for vertical sweeps, row for horizontal ones
+  for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+    bool ch = false;
+    // down: neighbours in the row above
+    for (int r = 0; r < RT; ++r) {
+      const T *up = s_out + r * PO + lane;  // (r-1, lane-1 .. lane+1) in interior coords
+      T nb = up[1];
+      if (CONN8) nb = Op<T, SUP>::apply(nb, Op<T, SUP>::apply(up[0], up[2]));
+      ch |= upd(r, lane, nb);
+      __syncwarp();
+    }
+    __syncthreads();
+    // up: neighbours in the row below
+    for (int r = RT - 1; r >= 0; --r) {
+      const T *dn = s_out + (r + 2) * PO + lane;
+      T nb = dn[1];
+      if (CONN8) nb = Op<T, SUP>::apply(nb, Op<T, SUP>::apply(dn[0], dn[2]));
+      ch |= upd(r, lane, nb);
+      __syncwarp();
+    }
+    __syncthreads();
+    // right: neighbours in the column to the left
+    for (int c = 0; c < RT; ++c) {
+      const T *lf = s_out + lane * PO + c;  // (lane-1 .. lane+1, c-1)
+      T nb = lf[PO];
+      if (CONN8) nb = Op<T, SUP>::apply(nb, Op<T, SUP>::apply(lf[0], lf[2 * PO]));
+      ch |= upd(lane, c, nb);
+      __syncwarp();
+    }
+    __syncthreads();
+    // left: neighbours in the column to the right
+    for (int c = RT - 1; c >= 0; --c) {
+      const T *rt = s_out + lane * PO + c + 2;
+      T nb = rt[PO];
+      if (CONN8) nb = Op<T, SUP>::apply(nb, Op<T, SUP>::apply(rt[0], rt[2 * PO]));
+      ch |= upd(lane, c, nb);
+      __syncwarp();
+    }
+    if (!__syncthreads_or(ch)) {
+      converged = true;
+      break;
+    }
+  }
+  if (!converged) bflags |= B_SELF;
+  if (bflags) atomicOr(s_flag, bflags);
+  __syncthreads();
+  const int f = *s_flag;
+
+  // write back (round 0 always: the marker itself is new) and flag the neighbours
+  T *rec = static_cast<T *>(im.rec);
+  if (round == 0 || f != 0) {
+    for (int i = threadIdx.x; i < RT * RT; i += RTHREADS) {
+      const int r = i / RT, c = i % RT;
+      const int64_t gy = y0 + r, gx = x0 + c;
+      if (gy < im.H && gx < im.W) st_cg(rec + gy * im.W + gx, s_out[(r + 1) * PO + (c + 1)]);
+    }
+  }
+  if (threadIdx.x == 0 && f != 0) {
+    unsigned *fnext = P.flags + (size_t)((round + 1) & 1) * P.ntiles;
+    auto flag = [&](int dx, int dy) {
+      const int nx = tx + dx, ny = ty + dy;
+      if (nx < 0 || ny < 0 || nx >= im.tiles_x || ny >= im.tiles_y) return;
+      fnext[im.tile_begin + ny * im.tiles_x + nx] = 1u;
+    };
+    if (f & B_N) flag(0, -1);
+    if (f & B_S) flag(0, 1);
+    if (f & B_W) flag(-1, 0);
+    if (f & B_E) flag(1, 0);
+    if (CONN8) {
+      if (f & B_NW) flag(-1, -1);
+      if (f & B_NE) flag(1, -1);
+      if (f & B_SW) flag(-1, 1);
+      if (f & B_SE) flag(1, 1);
+    }
+    if (f & B_SELF) flag(0, 0);
+    if (f & (B_N | B_S | B_W | B_E | B_SELF)) atomicExch(&P.ctl->any[(round + 1) % 3], 1u);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ const RImg &image_of(const RParams<T> &P, int tile, int &t_local) {
+  if (P.nimg == 1) { t_local = tile; return P.single; }
+  int lo = 0, hi = P.nimg - 1;
+  while (lo < hi) {  // last image whose tile_begin <= tile
+    const int mid = (lo + hi + 1) >> 1;
+    if (P.imgs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+  }
+  t_local = tile - P.imgs[lo].tile_begin;
+  return P.imgs[lo];
+}
+
+template <typename T, bool SUP, bool CONN8>
+__global__ void __launch_bounds__(tile_side<T>()) k_reconstruct(RParams<T> P) {
+  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  constexpr int PO = tile_pitch<T>(RT + 2);
+  constexpr int PM = tile_pitch<T>(RT);
+  __shared__ __align__(16) T s_out[(RT + 2) * PO];
+  __shared__ __align__(16) T s_mask[RT * PM];
+  __shared__ int s_flag;
+  __shared__ int s_active;
+  RCtl *ctl = P.ctl;
+
+  int round = 0;
+  bool ok = true;
+  for (;;) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->any[(round + 2) % 3] = 0u;
+    unsigned *fcur = P.flags + (size_t)(round & 1) * P.ntiles;
+    for (int t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+      if (threadIdx.x == 0) {
+        int a = 1;
+        if (round > 0) {
+          a = *((volatile unsigned *)(fcur + t)) != 0u;
+          if (a) fcur[t] = 0u;
+        }
+        s_active = a;
+      }
+      __syncthreads();
+      const bool active = s_active != 0;
+      __syncthreads();
+      if (active) {
+        int tl = 0;
+        const RImg &im = image_of(P, t, tl);
+        process_tile<T, SUP, CONN8>(im, P, tl, round, s_out, s_mask, &s_flag);
+      }
+    }
+    if (!grid_barrier(ctl)) { ok = false; break; }
+    const unsigned any = *((volatile unsigned *)&ctl->any[(round + 1) % 3]);
+    ++round;
+    if (!any) break;
+    if (round >= P.max_rounds) {
+      if (threadIdx.x == 0) set_status(ctl, PG_ERR_NOT_CONVERGED);
+      ok = false;
+      break;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->rounds = round;
+    g_recon_rounds = round;
+  }
+  if (!ok || P.epi == EPI_NONE) return;
+
+  // epilogue over every pixel of every image
+  const int64_t stride = (int64_t)gridDim.x * RTHREADS;
+  for (int k = 0; k < P.nimg; ++k) {
+    const RImg &im = (P.nimg == 1) ? P.single : P.imgs[k];
+    const int64_t n = im.H * im.W;
+    const T *rec = static_cast<const T *>(im.rec);
+    const T *ref = static_cast<const T *>(im.mask);
+    if (P.epi == EPI_BINARY_SUP) {
+      uint8_t *o = static_cast<uint8_t *>(im.out);
+      for (int64_t i = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; i < n; i += stride)
+        o[i] = (ldg(ref + i) > ld_cg(rec + i)) ? 255 : 0;
+    } else {  // EPI_CLIP_REF: low leveling min(rec, ref), high leveling max(rec, ref)
+      T *o = static_cast<T *>(im.out);
+      for (int64_t i = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; i < n; i += stride)
+        o[i] = Op<T, !SUP>::apply(ld_cg(rec + i), ldg(ref + i));
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+template <typename T, bool SUP, bool CONN8>
+static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool binary, cudaStream_t s) {
+  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  int ntiles = 0;
+  size_t rec_bytes = 0;
+  for (auto &im : imgs) {
+    im.tiles_x = (int)ceil_div(im.W, RT);
+    im.tiles_y = (int)ceil_div(im.H, RT);
+    im.tile_begin = ntiles;
+    ntiles += im.tiles_x * im.tiles_y;
+    if (binary) rec_bytes += (sizeof(T) * (size_t)(im.H * im.W) + 15) / 16 * 16;  // 16-byte aligned slots
+  }
+  if (ntiles == 0) return PG_OK;
+  const int nimg = (int)imgs.size();
+  // scratch: control block | flags | image table | reconstruction buffers (binary mode)
+  const size_t off_flags = 256;
+  const size_t off_tab = off_flags + ((sizeof(unsigned) * 2 * (size_t)ntiles + 255) / 256) * 256;
+  const size_t off_rec = off_tab + ((sizeof(RImg) * (size_t)(nimg > 1 ? nimg : 0) + 255) / 256) * 256;
+  const size_t total = off_rec + rec_bytes + 256;
+  Scratch scr;
+  PG_TRY(scr.alloc(total, s));
+  char *base = scr.as<char>();
+  if (binary) {
+    size_t off = off_rec;
+    for (auto &im : imgs) {
+      im.rec = base + off;
+      off += sizeof(T) * (size_t)(im.H * im.W);
+      off = (off + 15) / 16 * 16;
+    }
+  }
+  PG_CUDA_TRY(cudaMemsetAsync(base, 0, off_tab, s), "clear reconstruction control block");
+  std::vector<RImg> table;
+  if (nimg > 1) {
+    table = imgs;
+    PG_CUDA_TRY(cudaMemcpyAsync(base + off_tab, table.data(), sizeof(RImg) * (size_t)nimg, cudaMemcpyHostToDevice, s),
+                "upload image table");
+  }
+  RParams<T> P{};
+  P.single = imgs[0];
+  P.imgs = reinterpret_cast<const RImg *>(base + off_tab);
+  P.nimg = nimg;
+  P.ntiles = ntiles;
+  P.ctl = reinterpret_cast<RCtl *>(base);
+  P.flags = reinterpret_cast<unsigned *>(base + off_flags);
+  P.max_rounds = 16 + 4 * ntiles;
+  P.init = rq.init;
+  P.mask_mode = rq.mask_mode;
+  P.epi = rq.epi;
+  P.h = static_cast<T>(rq.h);
+
+  auto kern = k_reconstruct<T, SUP, CONN8>;
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  static std::mutex mu;
+  static int cached_dev = -1, cached_blocks = 0;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (cached_dev != dev) {
+      PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_blocks, kern, RTHREADS, 0), "occupancy");
+      cached_dev = dev;
+    }
+    per_sm = cached_blocks;
+  }
+  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
+  int grid = per_sm * num_sms();
+  if (grid > ntiles) grid = ntiles;
+
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(RTHREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P), "cooperative reconstruction launch");
+  return PG_OK;
+}
+
+template <typename T>
+static pg_status run_dispatch(std::vector<RImg> &imgs, const ReconRequest &rq, cudaStream_t s) {
+  const bool binary = rq.epi == EPI_BINARY_SUP;
+  if (rq.dilate) return rq.conn8 ? run_t<T, true, true>(imgs, rq, binary, s) : run_t<T, true, false>(imgs, rq, binary, s);
+  return rq.conn8 ? run_t<T, false, true>(imgs, rq, binary, s) : run_t<T, false, false>(imgs, rq, binary, s);
+}
+
+pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
+                                const ReconRequest &rq, cudaStream_t s) {
+  if (n_images < 1) return PG_OK;
+  std::vector<RImg> imgs((size_t)n_images);
+  for (int i = 0; i < n_images; ++i) {
+    const Dims d = dims_of(masks[i]);
+    RImg &im = imgs[(size_t)i];
+    im = RImg{};
+    im.marker = markers ? markers[i].data : nullptr;
+    im.mask = masks[i].data;
+    im.rec = outs[i].data;
+    im.out = outs[i].data;
+    im.H = d.nz * d.ny;  // rank 1: one row
+    im.W = d.nx;
+  }
+  PG_DISPATCH_PTYPE(masks[0].ptype, T, { return run_dispatch<T>(imgs, rq, s); });
+  return PG_OK;
+}
+
+}  // namespace pg
+
+extern "C" {
+
+// Synchronises `stream`, then reads and clears the device status of the reconstruction
+// kernels (PG_ERR_NOT_CONVERGED if one gave up since the last check).
+pg_status pg_check_device(pg_stream_t stream) {
+  PG_CUDA_TRY(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)), "stream synchronisation");
+  int st = 0, zero = 0;
+  PG_CUDA_TRY(cudaMemcpyFromSymbol(&st, pg::g_recon_status, sizeof(int)), "read device status");
+  if (st != 0) {
+    PG_CUDA_TRY(cudaMemcpyToSymbol(pg::g_recon_status, &zero, sizeof(int)), "clear device status");
+    return pg::fail(static_cast<pg_status>(st), "reconstruction did not converge within its round cap or wait limit");
+  }
+  return PG_OK;
+}
+
+int32_t pg_last_reconstruction_rounds(void) {
+  int r = -1;
+  if (cudaDeviceSynchronize() != cudaSuccess) return -1;
+  if (cudaMemcpyFromSymbol(&r, pg::g_recon_rounds, sizeof(int)) != cudaSuccess) return -1;
+  return r;
+}
+
+}  // extern "C"

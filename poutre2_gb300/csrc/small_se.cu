@@ -1,0 +1,223 @@
+// small_se.cu -- flat erosion/dilation by the predefined 3-tap / 3x3 / 3x3x3 structuring
+// elements, and by an arbitrary neighbour list.
+//
+// Reference: llm::details::t_ErodeDilateDispatcher specialisations
+// (low_level_morpho/details/ero_dil_static_se_t.hpp:298-915) and the runtime neighbour-list
+// dispatcher (ero_dil_runtime_nl_se_t.hpp:54-193).  All compute, per output pixel, the
+// min/max of the input over the SE's offsets that fall inside the image.
+//
+// GPU design: HBM-bound streaming.  A thread owns 16 contiguous bytes of a row (a Pack:
+// 16 u8, 8 u16, 4 i32/f32, 2 i64/f64) and a strip of rows (2D) or slices (3D); it slides a
+// three-row (three-slice) window down the strip, so every input byte is read from DRAM
+// once and every output byte written once.  The horizontal 3-neighbourhood of a pack comes
+// from its two edge neighbours (one scalar load each, L1 hits) and a funnel shift;
+// u8/u16 use the SIMD-in-word min/max.
+#include <vector>
+
+#include "common.cuh"
+
+namespace pg {
+
+enum { SH_SQUARE = 0, SH_CROSS = 1, SH_SEGX = 2, SH_SEGY = 3, SH_SEGZ = 4 };
+
+template <typename T> struct Scalar {
+  static constexpr int N = 1;
+  T e0;
+  __device__ __forceinline__ static Scalar load(const T *p) { Scalar r; r.e0 = ldg(p); return r; }
+  __device__ __forceinline__ void store(T *p) const { *p = e0; }
+  __device__ __forceinline__ static Scalar fill(T x) { Scalar r; r.e0 = x; return r; }
+  template <bool SUP> __device__ __forceinline__ static Scalar op(const Scalar &a, const Scalar &b) {
+    Scalar r; r.e0 = Op<T, SUP>::apply(a.e0, b.e0); return r;
+  }
+  __device__ __forceinline__ Scalar shl(T left) const { Scalar r; r.e0 = left; return r; }
+  __device__ __forceinline__ Scalar shr(T right) const { Scalar r; r.e0 = right; return r; }
+};
+
+// centre pack and its horizontal 3-neighbourhood of one row (neutral outside the image)
+template <typename T, bool SUP, typename P>
+__device__ __forceinline__ void load_row(const T *__restrict__ row, bool valid, int64_t x0, int64_t W, bool need_h,
+                                         P &c, P &h) {
+  const T NEU = Op<T, SUP>::neutral();
+  if (!valid) { c = P::fill(NEU); h = c; return; }
+  c = P::load(row + x0);
+  if (!need_h) { h = c; return; }
+  const T left = (x0 > 0) ? ldg(row + x0 - 1) : NEU;
+  const T right = (x0 + P::N < W) ? ldg(row + x0 + P::N) : NEU;
+  h = P::template op<SUP>(P::template op<SUP>(c, c.shl(left)), c.shr(right));
+}
+
+// 2D: SESquare2D / SECross2D / SESegmentX2D / SESegmentY2D (and SESegmentX1D as H == 1).
+template <typename T, bool SUP, int SHAPE, typename P>
+__global__ void __launch_bounds__(256) k_small2d(const T *__restrict__ in, T *__restrict__ out, int64_t H, int64_t W,
+                                                 int64_t npack, int R) {
+  const int64_t xp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t y0 = ((int64_t)blockIdx.y * blockDim.y + threadIdx.y) * R;
+  if (xp >= npack || y0 >= H) return;
+  const int64_t x0 = xp * P::N;
+  const int64_t y1 = (y0 + R < H) ? y0 + R : H;
+  constexpr bool NEED_H = (SHAPE != SH_SEGY);
+  P cp, hp, cc, hc, cn, hn;
+  load_row<T, SUP>(in + (y0 - 1) * W, y0 >= 1, x0, W, NEED_H, cp, hp);
+  load_row<T, SUP>(in + y0 * W, true, x0, W, NEED_H, cc, hc);
+  for (int64_t y = y0; y < y1; ++y) {
+    load_row<T, SUP>(in + (y + 1) * W, y + 1 < H, x0, W, NEED_H, cn, hn);
+    P r;
+    if constexpr (SHAPE == SH_SQUARE) r = P::template op<SUP>(P::template op<SUP>(hp, hc), hn);
+    else if constexpr (SHAPE == SH_CROSS) r = P::template op<SUP>(P::template op<SUP>(cp, hc), cn);
+    else if constexpr (SHAPE == SH_SEGX) r = hc;
+    else r = P::template op<SUP>(P::template op<SUP>(cp, cc), cn);
+    r.store(out + y * W + x0);
+    cp = cc; hp = hc; cc = cn; hc = hn;
+  }
+}
+
+// 3D: SESquare3D (26-conn.), SECross3D (6), SESegmentX3D/Y3D/Z3D.  out(z) = op(B(z-1), A(z), B(z+1))
+// with A the in-slice part and B the part taken from the adjacent slices.
+template <typename T, bool SUP, int SHAPE, typename P>
+__global__ void __launch_bounds__(256) k_small3d(const T *__restrict__ in, T *__restrict__ out, int64_t D, int64_t H,
+                                                 int64_t W, int64_t npack, int R) {
+  const int64_t xp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t y = (int64_t)blockIdx.y * blockDim.y + threadIdx.y;
+  const int64_t z0 = (int64_t)blockIdx.z * R;
+  if (xp >= npack || y >= H || z0 >= D) return;
+  const int64_t x0 = xp * P::N;
+  const int64_t z1 = (z0 + R < D) ? z0 + R : D;
+  const T NEU = Op<T, SUP>::neutral();
+  auto slice = [&](int64_t z, P &A, P &B) {
+    if (z < 0 || z >= D) { A = P::fill(NEU); B = A; return; }
+    const T *base = in + z * H * W;
+    P cu, hu, cm, hm, cd, hd;
+    const bool need_rows = (SHAPE == SH_SQUARE || SHAPE == SH_CROSS || SHAPE == SH_SEGY);
+    const bool need_h = (SHAPE != SH_SEGY && SHAPE != SH_SEGZ);
+    load_row<T, SUP>(base + y * W, true, x0, W, need_h, cm, hm);
+    if (need_rows) {
+      load_row<T, SUP>(base + (y - 1) * W, y >= 1, x0, W, SHAPE == SH_SQUARE, cu, hu);
+      load_row<T, SUP>(base + (y + 1) * W, y + 1 < H, x0, W, SHAPE == SH_SQUARE, cd, hd);
+    }
+    if constexpr (SHAPE == SH_SQUARE) { A = P::template op<SUP>(P::template op<SUP>(hu, hm), hd); B = A; }
+    else if constexpr (SHAPE == SH_CROSS) { A = P::template op<SUP>(P::template op<SUP>(cu, hm), cd); B = cm; }
+    else if constexpr (SHAPE == SH_SEGX) { A = hm; B = P::fill(NEU); }
+    else if constexpr (SHAPE == SH_SEGY) { A = P::template op<SUP>(P::template op<SUP>(cu, cm), cd); B = P::fill(NEU); }
+    else { A = cm; B = cm; }
+  };
+  P Ap, Bp, Ac, Bc, An, Bn;
+  slice(z0 - 1, Ap, Bp);
+  slice(z0, Ac, Bc);
+  for (int64_t z = z0; z < z1; ++z) {
+    slice(z + 1, An, Bn);
+    P r = P::template op<SUP>(P::template op<SUP>(Bp, Ac), Bn);
+    r.store(out + (z * H + y) * W + x0);
+    Ap = Ac; Bp = Bc; Ac = An; Bc = Bn;
+  }
+}
+
+// Arbitrary neighbour list, gather form with border clipping.
+template <typename T, bool SUP>
+__global__ void __launch_bounds__(256) k_nl(const T *__restrict__ in, T *__restrict__ out, int64_t D, int64_t H,
+                                            int64_t W, const int4 *__restrict__ offs, int n) {
+  const int64_t total = D * H * W;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = i % W, y = (i / W) % H, z = i / (W * H);
+    T v = Op<T, SUP>::neutral();
+    for (int k = 0; k < n; ++k) {
+      const int4 o = __ldg(offs + k);
+      const int64_t zz = z + o.x, yy = y + o.y, xx = x + o.z;
+      if (zz < 0 || yy < 0 || xx < 0 || zz >= D || yy >= H || xx >= W) continue;
+      v = Op<T, SUP>::apply(v, ldg(in + (zz * H + yy) * W + xx));
+    }
+    out[i] = v;
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+static int rows_per_thread(int64_t threads_without_strips, int64_t length, int cap) {
+  const int64_t target = (int64_t)num_sms() * 1024;
+  int64_t r = threads_without_strips * length / (target > 0 ? target : 1);
+  if (r < 1) r = 1;
+  if (r > cap) r = cap;
+  if (r > length) r = length;
+  return (int)r;
+}
+
+template <typename T, bool SUP, int SHAPE>
+static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream_t s) {
+  const bool vec = (W % Pack<T>::N == 0) && ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const int64_t npack = vec ? W / Pack<T>::N : W;
+  const int R = rows_per_thread(npack, H, 32);
+  dim3 block(32, 8);
+  dim3 grid((unsigned)ceil_div(npack, 32), (unsigned)ceil_div(ceil_div(H, R), 8));
+  if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the small-SE kernel");
+  if (vec) k_small2d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  else k_small2d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  return cuda_status(cudaGetLastError(), "small-SE 2D kernel launch");
+}
+
+template <typename T, bool SUP, int SHAPE>
+static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W, cudaStream_t s) {
+  const bool vec = (W % Pack<T>::N == 0) && ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const int64_t npack = vec ? W / Pack<T>::N : W;
+  const int R = rows_per_thread(npack * H, D, 16);
+  dim3 block(32, 8);
+  dim3 grid((unsigned)ceil_div(npack, 32), (unsigned)ceil_div(H, 8), (unsigned)ceil_div(D, R));
+  if (grid.y > 65535 || grid.z > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "volume too large for the small-SE kernel");
+  if (vec) k_small3d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  else k_small3d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  return cuda_status(cudaGetLastError(), "small-SE 3D kernel launch");
+}
+
+template <typename T, bool SUP>
+static pg_status small_dispatch(const pg_image &in, const pg_image &out, int se, cudaStream_t s) {
+  const Dims d = dims_of(in);
+  const T *src = static_cast<const T *>(in.data);
+  T *dst = static_cast<T *>(out.data);
+  if (d.count() == 0) return PG_OK;
+  switch (se) {
+    case PG_SE_SEGMENT_X_1D: return small2d_t<T, SUP, SH_SEGX>(src, dst, 1, d.nx, s);
+    case PG_SE_SQUARE_2D: return small2d_t<T, SUP, SH_SQUARE>(src, dst, d.ny, d.nx, s);
+    case PG_SE_CROSS_2D: return small2d_t<T, SUP, SH_CROSS>(src, dst, d.ny, d.nx, s);
+    case PG_SE_SEGMENT_X_2D: return small2d_t<T, SUP, SH_SEGX>(src, dst, d.ny, d.nx, s);
+    case PG_SE_SEGMENT_Y_2D: return small2d_t<T, SUP, SH_SEGY>(src, dst, d.ny, d.nx, s);
+    case PG_SE_SQUARE_3D: return small3d_t<T, SUP, SH_SQUARE>(src, dst, d.nz, d.ny, d.nx, s);
+    case PG_SE_CROSS_3D: return small3d_t<T, SUP, SH_CROSS>(src, dst, d.nz, d.ny, d.nx, s);
+    case PG_SE_SEGMENT_X_3D: return small3d_t<T, SUP, SH_SEGX>(src, dst, d.nz, d.ny, d.nx, s);
+    case PG_SE_SEGMENT_Y_3D: return small3d_t<T, SUP, SH_SEGY>(src, dst, d.nz, d.ny, d.nx, s);
+    case PG_SE_SEGMENT_Z_3D: return small3d_t<T, SUP, SH_SEGZ>(src, dst, d.nz, d.ny, d.nx, s);
+    default: return fail(PG_ERR_UNSUPPORTED_SE, "unsupported nl_static");
+  }
+}
+
+pg_status launch_small_se(const pg_image &in, const pg_image &out, int se, bool dilate, cudaStream_t s) {
+  PG_DISPATCH_PTYPE(in.ptype, T, {
+    return dilate ? small_dispatch<T, true>(in, out, se, s) : small_dispatch<T, false>(in, out, se, s);
+  });
+  return PG_OK;
+}
+
+pg_status launch_nl(const pg_image &in, const pg_image &out, const int32_t *offsets, int n, bool dilate,
+                    cudaStream_t s) {
+  const Dims d = dims_of(in);
+  if (d.count() == 0) return PG_OK;
+  // offsets -> (dz, dy, dx, 0) int4 in device memory.  The host copy is pageable: the
+  // runtime stages it before cudaMemcpyAsync returns, so it may be released right away.
+  Scratch dev;
+  PG_TRY(dev.alloc(sizeof(int4) * (size_t)n, s));
+  std::vector<int4> host((size_t)n);
+  for (int k = 0; k < n; ++k) {
+    int o[3] = {0, 0, 0};
+    for (int r = 0; r < in.rank; ++r) o[3 - in.rank + r] = offsets[k * in.rank + r];
+    host[(size_t)k] = make_int4(o[0], o[1], o[2], 0);
+  }
+  PG_CUDA_TRY(cudaMemcpyAsync(dev.ptr, host.data(), sizeof(int4) * (size_t)n, cudaMemcpyHostToDevice, s),
+              "copy of the offsets");
+  const int threads = 256;
+  int64_t blocks = ceil_div(d.count(), threads);
+  const int64_t cap = (int64_t)num_sms() * 16;
+  if (blocks > cap) blocks = cap;
+  PG_DISPATCH_PTYPE(in.ptype, T, {
+    if (dilate) k_nl<T, true><<<(unsigned)blocks, threads, 0, s>>>(static_cast<const T *>(in.data), static_cast<T *>(out.data), d.nz, d.ny, d.nx, dev.as<int4>(), n);
+    else k_nl<T, false><<<(unsigned)blocks, threads, 0, s>>>(static_cast<const T *>(in.data), static_cast<T *>(out.data), d.nz, d.ny, d.nx, dev.as<int4>(), n);
+  });
+  return cuda_status(cudaGetLastError(), "neighbour-list kernel launch");
+}
+
+}  // namespace pg

@@ -1,0 +1,110 @@
+"""geodesy on device images, mirroring poutre2's public API (poutre::geo).
+
+include/poutre/geodesy/mreconstruct.hpp:37-41, extrema.hpp:33-64, leveling.hpp:37-52.
+The kernels run asynchronously on the current CUDA stream; with ``sync_checks`` on (the
+default) each call then waits for its stream and raises ``PoutreError`` if the device gave
+up (round cap / bounded wait), as the synchronous reference would throw.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from typing import Sequence
+
+import torch
+
+from . import _lib
+from .image import descriptor
+from .se import Common_NL_SE
+
+sync_checks = True
+
+
+class reconstruction_type(enum.IntEnum):
+    """poutre::geo::reconstruction_type (mreconstruct.hpp:28-31)."""
+    erode = 0
+    dilate = 1
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _post(check):
+    if sync_checks if check is None else check:
+        _lib.call("pg_check_device", _stream())
+
+
+def Reconstruction(rect_type, i_marker, i_mask, nl_static, o_img, check=None):
+    dm, dk, do = descriptor(i_marker, "marker"), descriptor(i_mask, "mask"), descriptor(o_img, "output")
+    _lib.call("pg_reconstruction", int(reconstruction_type(rect_type)), ctypes.byref(dm), ctypes.byref(dk),
+              int(Common_NL_SE(nl_static)), ctypes.byref(do), _stream())
+    _post(check)
+
+
+def _extrema(name, i_img, pvalue, nl_static, o_img, check):
+    di, do = descriptor(i_img, "input"), descriptor(o_img, "output")
+    _lib.call(name, ctypes.byref(di), float(pvalue), int(Common_NL_SE(nl_static)), ctypes.byref(do), _stream())
+    _post(check)
+
+
+def h_minima(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_h_minima", i_img, pvalue, nl_static, o_img, check)
+
+
+def h_maxima(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_h_maxima", i_img, pvalue, nl_static, o_img, check)
+
+
+def h_convex(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_h_convex", i_img, pvalue, nl_static, o_img, check)
+
+
+def h_concave(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_h_concave", i_img, pvalue, nl_static, o_img, check)
+
+
+def dynamic_pseudo_opening(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_dynamic_pseudo_opening", i_img, pvalue, nl_static, o_img, check)
+
+
+def dynamic_pseudo_closing(i_img, pvalue, nl_static, o_img, check=None):
+    _extrema("pg_dynamic_pseudo_closing", i_img, pvalue, nl_static, o_img, check)
+
+
+def h_maxima_binary(i_img, pvalue, nl_static, o_img, check=None):
+    """o_img (uint8) = 255 where i_img > h_maxima(i_img) else 0, one fused launch."""
+    _extrema("pg_h_maxima_binary", i_img, pvalue, nl_static, o_img, check)
+
+
+def h_maxima_binary_batch(imgs: Sequence[torch.Tensor], pvalue, nl_static, outs: Sequence[torch.Tensor], check=None):
+    """Binary h-maxima of a ragged list of 2D images in one persistent launch."""
+    n = len(imgs)
+    if len(outs) != n:
+        raise _lib.PoutreError(1, "h_maxima_binary_batch: as many outputs as inputs are needed")
+    ins = (_lib.PgImage * n)(*[descriptor(t, "input") for t in imgs])
+    ous = (_lib.PgImage * n)(*[descriptor(t, "output") for t in outs])
+    _lib.call("pg_h_maxima_binary_batch", ins, ous, n, float(pvalue), int(Common_NL_SE(nl_static)), _stream())
+    _post(check)
+
+
+def _leveling(name, i_ref, i_marker, nl_static, o_img, check):
+    dr, dm, do = descriptor(i_ref, "ref"), descriptor(i_marker, "marker"), descriptor(o_img, "output")
+    _lib.call(name, ctypes.byref(dr), ctypes.byref(dm), int(Common_NL_SE(nl_static)), ctypes.byref(do), _stream())
+    _post(check)
+
+
+def low_leveling(i_ref, i_marker, nl_static, o_img, check=None):
+    _leveling("pg_low_leveling", i_ref, i_marker, nl_static, o_img, check)
+
+
+def high_leveling(i_ref, i_marker, nl_static, o_img, check=None):
+    _leveling("pg_high_leveling", i_ref, i_marker, nl_static, o_img, check)
+
+
+def leveling(i_ref, i_marker, nl_static, o_img, check=None):
+    _leveling("pg_leveling", i_ref, i_marker, nl_static, o_img, check)
+
+
+def last_reconstruction_rounds() -> int:
+    return int(_lib.load().pg_last_reconstruction_rounds())

@@ -1,0 +1,86 @@
+"""CPU-side checks of the boundary: the C-ABI library builds for sm_103a, loads without a GPU
+and exports exactly the entry points include/poutre_gb300.h declares; host-side helpers."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "poutre_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^PG_API\s+[^;(]*?\b(pg_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from poutre2_gb300 import build
+    return build.build()
+
+
+def test_header_declares_the_boundary():
+    syms = declared_symbols()
+    from poutre2_gb300._lib import EXPORTED
+    assert syms == sorted(EXPORTED)
+    assert len(syms) >= 30
+
+
+def test_library_loads_and_exports_every_declared_symbol(lib_path):
+    lib = ctypes.CDLL(lib_path)
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True).stdout
+    exported = sorted(l.split()[-1] for l in out.splitlines() if l.split()[-1].startswith("pg_"))
+    assert exported == declared_symbols()
+
+
+def test_library_is_built_for_sm_103a(lib_path):
+    from poutre2_gb300 import build
+    assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+
+
+def test_python_binding_loads_without_gpu(lib_path):
+    from poutre2_gb300 import _lib
+    L = _lib.load()
+    assert b"sm_103a" in L.pg_version()
+
+
+def test_descriptor_rejects_cpu_tensors():
+    import torch
+    from poutre2_gb300._lib import PoutreError
+    from poutre2_gb300.image import descriptor
+    with pytest.raises(PoutreError):
+        descriptor(torch.zeros(4, 4, dtype=torch.uint8))
+
+
+def test_image_string_round_trip_host():
+    from poutre2_gb300.image import ImageFromString, ImageToString
+    s = "Scalar GINT64 2 2 3 1 -2 3 4 5 6"
+    t = ImageFromString(s, device="cpu")
+    assert t.shape == (2, 3) and ImageToString(t) == s
+    # trailing tokens are ignored, as poutre::ImageFromString does
+    assert ImageToString(ImageFromString("Scalar GUINT8 1 3 1 2 3 9 9", device="cpu")) == "Scalar GUINT8 1 3 1 2 3"
+
+
+def test_structuring_elements():
+    from poutre2_gb300.se import NeighborList, predefined_offsets
+    assert len(predefined_offsets("SESquare3D")) == 27 and predefined_offsets("SESquare2D")[0] == (0, 0)
+    seg = NeighborList.segment(-1, 1, 31)
+    assert len(seg) == 63 and (-31, 31) in seg.offsets and (31, -31) in seg.offsets
+    lo, hi = NeighborList.rectangle(2, 3).maximum_extension()
+    assert lo == (-2, -3) and hi == (2, 3)
+    assert NeighborList([(1, 2)]).Transpose().offsets == [(-1, -2)]
+
+
+def test_synthetic_inputs_are_deterministic():
+    from poutre2_gb300 import synthetic
+    a = synthetic.smoothed_noise_u8((64, 80), 1)
+    b = synthetic.smoothed_noise_u8((64, 80), 1)
+    assert np.array_equal(a, b) and a.min() == 0 and a.max() == 255
+    sizes = synthetic.ragged_sizes(512)
+    assert len(sizes) == 512 and all(64 <= h <= 1024 and 64 <= w <= 1024 for h, w in sizes)

@@ -1,0 +1,415 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's known answers and
+against the oracle on seeded random inputs.  Integer, byte and float min/max results must be
+bit-exact (tolerance 0)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests.kats import case_id, load_cases, to_array
+
+pytestmark = pytest.mark.gpu
+
+TYPES = [np.uint8, np.uint16, np.int32, np.int64, np.float32, np.float64]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from poutre2_gb300 import _lib
+    _lib.load()
+    yield
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def rand(rng, shape, dt):
+    dt = np.dtype(dt)
+    if dt.kind == "f":
+        return rng.standard_normal(shape).astype(dt)
+    info = np.iinfo(dt)
+    lo, hi = max(info.min, -100000), min(info.max, 100000)
+    if dt == np.uint8:
+        lo, hi = 0, 255
+    return rng.integers(lo, hi + 1, shape, dtype=np.int64).astype(dt)
+
+
+# ----------------------------------------------------------------------------- known answers
+CASES = load_cases()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[case_id(c) for c in CASES])
+def test_reference_kat_on_gpu(case):
+    from poutre2_gb300 import geo, llm
+    from poutre2_gb300.se import Common_NL_SE, NeighborList
+    ins = [dev(to_array(i)) for i in case["inputs"]]
+    exp = to_array(case["expected"])
+    out = torch.empty_like(ins[0])
+    op = case["op"]
+    if op in ("dilate_static", "erode_static"):
+        (llm.Dilate if op.startswith("dilate") else llm.Erode)(ins[0], Common_NL_SE[case["se"]], 1, out)
+    elif op in ("dilate_nl", "erode_nl"):
+        (llm.Dilate if op.startswith("dilate") else llm.Erode)(ins[0], NeighborList.predefined(case["se"]), out)
+    elif op in ("dilatex", "erodex", "dilatey", "erodey"):
+        fn = {"dilatex": llm.DilateX, "erodex": llm.ErodeX, "dilatey": llm.DilateY, "erodey": llm.ErodeY}[op]
+        fn(ins[0], case["half"], out)
+    elif op.startswith("reconstruct_"):
+        geo.Reconstruction(geo.reconstruction_type.dilate if op.endswith("dilate") else geo.reconstruction_type.erode,
+                           ins[0], ins[1], Common_NL_SE[case["se"]], out)
+    elif op in ("low_leveling", "high_leveling", "leveling"):
+        getattr(geo, op)(ins[0], ins[1], Common_NL_SE[case["se"]], out)
+    else:
+        getattr(geo, op)(ins[0], case["h"], Common_NL_SE[case["se"]], out)
+    np.testing.assert_array_equal(host(out), exp)
+
+
+# ----------------------------------------------------------------------------- static SEs
+SHAPES_2D = [(1, 1), (1, 37), (29, 1), (5, 5), (17, 33), (64, 64), (127, 130), (256, 48)]
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("se", ["SESquare2D", "SECross2D", "SESegmentX2D", "SESegmentY2D"])
+def test_static_2d_random(dt, se):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(abs(hash((se, str(dt)))) % 2**32)
+    for shape in SHAPES_2D:
+        a = rand(rng, shape, dt)
+        x = dev(a)
+        for it in (1, 2, 3):
+            for dil in (True, False):
+                out = torch.empty_like(x)
+                (llm.Dilate if dil else llm.Erode)(x, Common_NL_SE[se], it, out)
+                np.testing.assert_array_equal(host(out), oracle.erode_dilate_static(a, se, it, dil),
+                                              err_msg=f"{se} {shape} iter={it} dilate={dil}")
+
+
+def test_static_unaligned_views_use_scalar_path():
+    # a row width that is not a multiple of 16 bytes and a 16-byte-misaligned base
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(3)
+    a = rand(rng, (40, 50), np.uint8)
+    big = torch.zeros(40 * 50 + 3, dtype=torch.uint8, device="cuda")
+    x = big[3:].view(40, 50)
+    x.copy_(dev(a))
+    out = torch.empty_like(x)
+    llm.Dilate(x, Common_NL_SE.SESquare2D, 1, out)
+    np.testing.assert_array_equal(host(out), oracle.dilate(a, "SESquare2D"))
+
+
+@pytest.mark.parametrize("se", ["SESegmentX1D"])
+@pytest.mark.parametrize("dt", TYPES)
+def test_static_1d(se, dt):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(1)
+    for n in (1, 2, 15, 16, 17, 1000):
+        a = rand(rng, (n,), dt)
+        x = dev(a)
+        out = torch.empty_like(x)
+        llm.Dilate(x, Common_NL_SE[se], 2, out)
+        np.testing.assert_array_equal(host(out), oracle.erode_dilate_static(a, se, 2, True))
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32])
+@pytest.mark.parametrize("se", ["SESquare3D", "SECross3D", "SESegmentX3D", "SESegmentY3D", "SESegmentZ3D"])
+def test_static_3d(dt, se):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(5)
+    for shape in [(1, 1, 1), (3, 3, 3), (5, 7, 9), (17, 20, 64), (2, 33, 31)]:
+        a = rand(rng, shape, dt)
+        x = dev(a)
+        for dil in (True, False):
+            out = torch.empty_like(x)
+            (llm.Dilate if dil else llm.Erode)(x, Common_NL_SE[se], 1, out)
+            np.testing.assert_array_equal(host(out), oracle.erode_dilate_static(a, se, 1, dil), err_msg=f"{shape}")
+
+
+@pytest.mark.parametrize("cse,rank", [("Octagon", 2), ("Rhombicuboctahedron", 3)])
+def test_compound(cse, rank):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Compound_NL_SE
+    rng = np.random.default_rng(8)
+    shape = (40, 45) if rank == 2 else (12, 13, 14)
+    a = rand(rng, shape, np.int32)
+    x = dev(a)
+    cross, square = ("SECross2D", "SESquare2D") if rank == 2 else ("SECross3D", "SESquare3D")
+    for size in (0, 2, 3, 5, 8):
+        out = torch.empty_like(x)
+        llm.Dilate(x, Compound_NL_SE[cse], size, out)
+        nb = size / (1 + 2 ** 0.5)
+        nsq = int(np.floor(nb) if nb - np.floor(nb) < 0.5 else np.floor(nb) + 1)
+        exp = a.copy()
+        for p in ([cross] * (size - nsq) + [square] * nsq) if size else []:
+            exp = oracle.dilate(exp, p, 1)
+        np.testing.assert_array_equal(host(out), exp, err_msg=f"size={size}")
+
+
+# ----------------------------------------------------------------------------- neighbour lists, lines
+@pytest.mark.parametrize("dt", TYPES)
+def test_neighbor_list(dt):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import NeighborList
+    rng = np.random.default_rng(2)
+    a = rand(rng, (45, 70), dt)
+    x = dev(a)
+    for nl in (NeighborList.segment(-1, 1, 7), NeighborList.rectangle(2, 2), NeighborList([(0, 3), (-2, -1)])):
+        for dil in (True, False):
+            out = torch.empty_like(x)
+            (llm.Dilate if dil else llm.Erode)(x, nl, out)
+            np.testing.assert_array_equal(host(out), oracle.erode_dilate_nl(a, nl.offsets, dil))
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("half", [1, 2, 7, 31, 200])
+def test_lines_xy(dt, half):
+    from poutre2_gb300 import llm
+    rng = np.random.default_rng(half)
+    for shape in [(1, 300), (37, 37), (130, 130)]:
+        a = rand(rng, shape, dt)
+        x = dev(a)
+        for name, axis in (("X", "x"), ("Y", "y")):
+            if axis == "y" and shape[0] != shape[1]:
+                continue
+            for dil in (True, False):
+                out = torch.empty_like(x)
+                getattr(llm, ("Dilate" if dil else "Erode") + name)(x, half, out)
+                np.testing.assert_array_equal(host(out), oracle.line(a, half, axis, dil), err_msg=f"{name} {shape}")
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.float32, np.float64])
+@pytest.mark.parametrize("d", [(0, 1), (1, 0), (-1, 1), (1, 1)])
+@pytest.mark.parametrize("half", [1, 5, 31])
+def test_segments_any_direction(dt, d, half):
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import NeighborList
+    rng = np.random.default_rng(half * 7 + d[0] * 3 + d[1])
+    a = rand(rng, (77, 150), dt)
+    x = dev(a)
+    offs = NeighborList.segment(d[0], d[1], half).offsets
+    for dil in (True, False):
+        out = torch.empty_like(x)
+        (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_line(d[0], d[1], half), out)
+        np.testing.assert_array_equal(host(out), oracle.erode_dilate_nl(a, offs, dil))
+
+
+@pytest.mark.parametrize("dt", [np.uint16, np.float32])
+def test_rect_and_composites(dt):
+    from poutre2_gb300 import llm
+    rng = np.random.default_rng(4)
+    a = rand(rng, (150, 170), dt)
+    x = dev(a)
+    for hy, hx in ((15, 15), (0, 4), (3, 0), (2, 9)):
+        se = llm.se_rect(hy, hx)
+        d, e = oracle.rect(a, hy, hx, True), oracle.rect(a, hy, hx, False)
+        for fn, exp in ((llm.DilateSE, d), (llm.ErodeSE, e), (llm.Opening, oracle.rect(e, hy, hx, True)),
+                        (llm.Closing, oracle.rect(d, hy, hx, False)), (llm.Gradient, (d - e).astype(a.dtype))):
+            out = torch.empty_like(x)
+            fn(x, se, out)
+            np.testing.assert_array_equal(host(out), exp, err_msg=f"{fn.__name__} {hy}x{hx}")
+
+
+def test_square_iterated_equals_rect_on_gpu():
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(6)
+    a = rand(rng, (100, 90), np.float32)
+    x = dev(a)
+    o1, o2 = torch.empty_like(x), torch.empty_like(x)
+    llm.Dilate(x, Common_NL_SE.SESquare2D, 15, o1)
+    llm.DilateSE(x, llm.se_rect(15, 15), o2)
+    np.testing.assert_array_equal(host(o1), host(o2))
+
+
+# ----------------------------------------------------------------------------- geodesy
+def smooth(rng_seed, shape, sigma=3.0):
+    from poutre2_gb300 import synthetic
+    return synthetic.smoothed_noise_u8(shape, rng_seed, sigma)
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("se", ["SESquare2D", "SECross2D"])
+def test_reconstruction(dt, se):
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    for k, shape in enumerate([(1, 1), (1, 100), (100, 1), (63, 65), (64, 64), (200, 333)]):
+        mask = smooth(k, shape).astype(dt)
+        rng = np.random.default_rng(k)
+        marker = (mask.astype(np.float64) - rng.integers(0, 40, shape)).astype(np.float64)
+        marker = np.clip(marker, 0, None).astype(dt)
+        for dil in (True, False):
+            mk = marker if dil else np.minimum(mask.astype(np.float64) + 30, 255).astype(dt)
+            out = torch.empty_like(dev(mask))
+            geo.Reconstruction(geo.reconstruction_type.dilate if dil else geo.reconstruction_type.erode,
+                               dev(mk), dev(mask), Common_NL_SE[se], out)
+            np.testing.assert_array_equal(host(out), oracle.reconstruct(mk, mask, se, dil), err_msg=f"{shape} {dil}")
+
+
+def test_reconstruction_long_geodesic_paths():
+    # a serpentine corridor forces propagation through many tiles and rounds
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    H, W = 300, 260
+    mask = np.zeros((H, W), np.uint8)
+    for r in range(0, H, 4):
+        mask[r, :] = 200
+        c = W - 1 if (r // 4) % 2 == 0 else 0
+        mask[r:r + 4, c] = 200
+    marker = np.zeros_like(mask)
+    marker[0, 0] = 200
+    for se in ("SESquare2D", "SECross2D"):
+        out = torch.empty_like(dev(mask))
+        geo.Reconstruction(geo.reconstruction_type.dilate, dev(marker), dev(mask), Common_NL_SE[se], out)
+        np.testing.assert_array_equal(host(out), oracle.reconstruct(marker, mask, se, True))
+
+
+def test_reconstruction_1d():
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(0)
+    mask = rng.integers(0, 255, 5000).astype(np.uint8)
+    marker = (mask // 3).astype(np.uint8)
+    out = torch.empty_like(dev(mask))
+    geo.Reconstruction(geo.reconstruction_type.dilate, dev(marker), dev(mask), Common_NL_SE.SESegmentX1D, out)
+    np.testing.assert_array_equal(host(out), oracle.reconstruct(marker, mask, "SESegmentX1D", True))
+
+
+@pytest.mark.parametrize("kind", ["h_minima", "h_maxima", "h_convex", "h_concave", "dynamic_pseudo_opening",
+                                  "dynamic_pseudo_closing"])
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.int64])
+def test_extrema(kind, dt):
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    f = smooth(11, (150, 210)).astype(dt)
+    for se in ("SESquare2D", "SECross2D"):
+        out = torch.empty_like(dev(f))
+        getattr(geo, kind)(dev(f), 10, Common_NL_SE[se], out)
+        np.testing.assert_array_equal(host(out), getattr(oracle, kind)(f, 10, se), err_msg=se)
+
+
+def test_h_maxima_binary_and_batch():
+    from poutre2_gb300 import geo, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    imgs = [synthetic.smoothed_noise_u8(hw, 100 + i) for i, hw in enumerate([(64, 64), (65, 300), (1, 5), (333, 97),
+                                                                             (128, 128), (7, 700)])]
+    outs = [torch.empty_like(dev(f)) for f in imgs]
+    geo.h_maxima_binary_batch([dev(f) for f in imgs], 10, Common_NL_SE.SESquare2D, outs)
+    for f, o in zip(imgs, outs):
+        np.testing.assert_array_equal(host(o), oracle.h_maxima_binary(f, 10))
+        single = torch.empty_like(o)
+        geo.h_maxima_binary(dev(f), 10, Common_NL_SE.SESquare2D, single)
+        np.testing.assert_array_equal(host(single), host(o))
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("kind", ["low_leveling", "high_leveling", "leveling"])
+def test_leveling(dt, kind):
+    from poutre2_gb300 import geo, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    ref = smooth(21, (140, 190)).astype(dt)
+    marker = synthetic.leveling_marker(smooth(21, (140, 190)), 6.0).astype(dt)
+    for se in ("SESquare2D", "SECross2D"):
+        out = torch.empty_like(dev(ref))
+        getattr(geo, kind)(dev(ref), dev(marker), Common_NL_SE[se], out)
+        np.testing.assert_array_equal(host(out), getattr(oracle, kind)(ref, marker, se), err_msg=se)
+
+
+# ----------------------------------------------------------------------------- adjoint
+@pytest.mark.parametrize("dilate", [True, False])
+@pytest.mark.parametrize("r", [1, 2, 3])
+def test_flat_forward_backward_exact(dilate, r):
+    from poutre2_gb300 import autograd
+    rng = np.random.default_rng(r)
+    x = rng.standard_normal((2, 3, 37, 70)).astype(np.float32)
+    x[0, 0, 5, :] = 0.5  # plateaus exercise the first-in-scan-order tie rule
+    g = rng.standard_normal(x.shape).astype(np.float32)
+    xt = dev(x)
+    y = autograd.flat_forward(xt, r, dilate)
+    np.testing.assert_array_equal(host(y), oracle.flat2d_forward(x, r, dilate))
+    gx = autograd.flat_backward(xt, dev(g), r, dilate)
+    np.testing.assert_array_equal(host(gx), oracle.flat2d_backward(x, g, r, dilate))
+
+
+def test_opening_autograd_matches_oracle_chain():
+    from poutre2_gb300 import autograd
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((2, 2, 40, 50)).astype(np.float32)
+    g = rng.standard_normal(x.shape).astype(np.float32)
+    xt = dev(x).requires_grad_(True)
+    y = autograd.opening(xt, 2)
+    y.backward(dev(g))
+    e = oracle.flat2d_forward(x, 2, False)
+    np.testing.assert_array_equal(host(y.detach()), oracle.flat2d_forward(e, 2, True))
+    ge = oracle.flat2d_backward(e, g, 2, True)
+    np.testing.assert_array_equal(host(xt.grad), oracle.flat2d_backward(x, ge, 2, False))
+
+
+def test_dilation_gradient_finite_differences():
+    from poutre2_gb300 import autograd
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((1, 1, 24, 24)).astype(np.float64)
+    g = rng.standard_normal(x.shape)
+    r, eps = 2, 1e-3
+    xt = dev(x.astype(np.float32)).requires_grad_(True)
+    y = autograd.dilation(xt, r)
+    y.backward(dev(g.astype(np.float32)))
+    grad = host(xt.grad).astype(np.float64)
+    x32 = x.astype(np.float32)
+    # pixels whose every window max is unique by a margin > 1e-2
+    H, W = x.shape[-2:]
+    checked = 0
+    for q in rng.permutation(H * W)[:60]:
+        qy, qx = divmod(int(q), W)
+        ok = True
+        for py in range(max(0, qy - r), min(H, qy + r + 1)):
+            for px in range(max(0, qx - r), min(W, qx + r + 1)):
+                win = np.sort(x32[0, 0, max(0, py - r):py + r + 1, max(0, px - r):px + r + 1].ravel())
+                if win.size > 1 and win[-1] - win[-2] <= 1e-2:
+                    ok = False
+        if not ok:
+            continue
+        def loss(v):
+            xx = x32.copy()
+            xx[0, 0, qy, qx] = np.float32(v)
+            out = host(autograd.flat_forward(dev(xx), r, True)).astype(np.float64)
+            return float((out * g).sum())
+        fd = (loss(x32[0, 0, qy, qx] + eps) - loss(x32[0, 0, qy, qx] - eps)) / (2 * eps)
+        assert abs(fd - grad[0, 0, qy, qx]) <= 1e-3 * max(1.0, abs(fd)), (qy, qx, fd, grad[0, 0, qy, qx])
+        checked += 1
+    assert checked >= 10
+
+
+# ----------------------------------------------------------------------------- errors
+def test_errors_mirror_reference_checks():
+    from poutre2_gb300 import geo, llm
+    from poutre2_gb300._lib import PoutreError
+    from poutre2_gb300.se import Common_NL_SE
+    x = torch.zeros((8, 9), dtype=torch.uint8, device="cuda")
+    with pytest.raises(PoutreError, match="ALIASING"):
+        llm.Dilate(x, Common_NL_SE.SESquare2D, 1, x)
+    with pytest.raises(PoutreError, match="INCOMPATIBLE"):
+        llm.Dilate(x, Common_NL_SE.SESquare2D, 1, torch.zeros((9, 8), dtype=torch.uint8, device="cuda"))
+    with pytest.raises(PoutreError, match="INCOMPATIBLE"):
+        llm.Dilate(x, Common_NL_SE.SESquare2D, 1, torch.zeros((8, 9), dtype=torch.int32, device="cuda"))
+    with pytest.raises(PoutreError, match="UNSUPPORTED_SE"):
+        llm.Dilate(x, Common_NL_SE.SESquare3D, 1, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="INVALID_ARGUMENT"):
+        llm.Dilate(x, Common_NL_SE.SESquare2D, -1, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="NOT_SQUARE"):
+        llm.DilateY(x, 2, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="INVALID_ARGUMENT"):
+        geo.h_maxima(x, 3.5, Common_NL_SE.SESquare2D, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="INVALID_ARGUMENT"):
+        geo.h_maxima(x, -1, Common_NL_SE.SESquare2D, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="UNSUPPORTED_SE"):
+        geo.Reconstruction(geo.reconstruction_type.dilate, x, x.clone(), Common_NL_SE.SESegmentX2D, torch.empty_like(x))
+    with pytest.raises(PoutreError):
+        llm.Dilate(x.cpu(), Common_NL_SE.SESquare2D, 1, torch.empty_like(x))
