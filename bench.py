@@ -220,6 +220,8 @@ def run_gpu(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        time.sleep(0.5)  # let the sampler take its first readings before the timed steps
+        torch.cuda.synchronize()
         for i in range(args.steps):
             flush_l2(flush)
             ev[i][0].record(stream)
@@ -282,7 +284,7 @@ def run_gpu(args):
         "gpu_launches": args.steps,  # one persistent k_reconstruct launch per step (plus one memset)
         "clocks": clocks,
     }
-    if rank == 0:
+    if rank == 0 and not args.no_cpu:
         v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
         line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
                                 "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
@@ -304,6 +306,7 @@ def main():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--extra", action="store_true", help="also measure the other workloads")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -291,10 +291,18 @@ def gradient_from(dil, ero):
     return (dil - ero).astype(dil.dtype)
 
 
+def line_y_any(img, half: int, dilate: bool = True) -> np.ndarray:
+    """Vertical running min/max of any 2D image: the X restatement on the transposed image.
+    (The reference's DilateY only accepts square images; the window itself does not care.)"""
+    a = _c(img)
+    return np.ascontiguousarray(line(np.ascontiguousarray(a.T), half, "x", dilate).T)
+
+
 def rect(img, hy, hx, dilate=True):
-    """Flat (2hy+1)x(2hx+1) rectangle = DilateY(DilateX(.)) (ero_dil_line_se_t.hpp)."""
+    """Flat (2hy+1)x(2hx+1) rectangle = Y(hy) o X(hx) running min/max; equals the reference's
+    DilateY(DilateX(.)) and Dilate(SESquare2D, iter=h) for hy == hx == h."""
     t = line(img, hx, "x", dilate) if hx > 0 else _c(img).copy()
-    return line(t, hy, "y", dilate) if hy > 0 else t
+    return line_y_any(t, hy, dilate) if hy > 0 else t
 
 
 # ----------------------------------------------------------------------------- adjoint

@@ -134,15 +134,22 @@ static pg_status line_t(const T *in, T *out, int64_t H, int64_t W, int dy, int d
   const size_t budget = 96 * 1024, hard = 227 * 1024;
   LineGeom g{};
   bool ok = false;
+  // largest tile whose staged region fits the budget; narrower tiles for very long segments
   if (dy == 0) {
-    for (int ty : {16, 8, 4, 2, 1}) {
-      g = make_geom(0, 1, k, ty, 256);
-      if (line_smem(g, sizeof(T)) <= budget) { ok = true; break; }
+    for (int tx : {256, 128, 64, 32}) {
+      for (int ty : {16, 8, 4, 2, 1}) {
+        g = make_geom(0, 1, k, ty, tx);
+        if (line_smem(g, sizeof(T)) <= budget) { ok = true; break; }
+      }
+      if (ok) break;
     }
   } else if (dx == 0) {
-    for (int ty : {256, 128, 64, 32, 16, 8, 4, 2, 1}) {
-      g = make_geom(1, 0, k, ty, 64);
-      if (line_smem(g, sizeof(T)) <= budget) { ok = true; break; }
+    for (int tx : {64, 32, 16, 8}) {
+      for (int ty : {256, 128, 64, 32, 16, 8, 4, 2, 1}) {
+        g = make_geom(1, 0, k, ty, tx);
+        if (line_smem(g, sizeof(T)) <= budget) { ok = true; break; }
+      }
+      if (ok) break;
     }
   } else {
     for (int t : {128, 64, 32, 16, 8, 4, 2, 1}) {

@@ -443,7 +443,10 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   P.ntiles = ntiles;
   P.ctl = reinterpret_cast<RCtl *>(base);
   P.flags = reinterpret_cast<unsigned *>(base + off_flags);
-  P.max_rounds = 16 + 4 * ntiles;
+  // A round moves information across at least one tile border, so the rounds needed are
+  // bounded by the tile crossings of the longest geodesic path; the cap only guards against
+  // a runaway (termination is guaranteed: every round raises some pixel to another input value).
+  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)ntiles);
   P.init = rq.init;
   P.mask_mode = rq.mask_mode;
   P.epi = rq.epi;
