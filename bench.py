@@ -175,8 +175,140 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def _time_ms(fn, flush, reps=5, warm=2):
+    """Median CUDA-event time of fn() on the current stream, L2 flushed before each rep."""
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    out = []
+    for _ in range(reps):
+        flush_l2(flush)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        fn()
+        b.record(st)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.median(out)
+
+
 def extra_measurements(dev, flush):
-    return {}
+    """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way."""
+    import numpy as np
+    import torch
+
+    from poutre2_gb300 import autograd, geo, llm, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    peak, _ = peaks()
+    res = {}
+
+    def rec(name, ms, pixels, alg_bytes, **kw):
+        d = {"ms": round(ms, 5), "Gpixel_s": pixels / ms / 1e6}
+        if alg_bytes:
+            d["GB_s"] = alg_bytes / ms / 1e6
+            d["hbm_frac"] = d["GB_s"] / peak
+        d.update(kw)
+        res[name] = d
+
+    def guard(fn):
+        try:
+            fn()
+        except Exception as e:  # keep the headline line even if an extra fails
+            res.setdefault("errors", []).append(f"{fn.__name__}: {type(e).__name__}: {e}")
+
+    def cfg1():
+        x = torch.from_numpy(synthetic.uniform_u8((512, 512), 0)).to(dev)
+        o = torch.empty_like(x)
+        for se in ("SESquare2D", "SECross2D"):
+            for dil in (True, False):
+                f = (lambda s=se, d=dil: (llm.Dilate if d else llm.Erode)(x, Common_NL_SE[s], 1, o))
+                rec(f"cfg1_{'dilate' if dil else 'erode'}_{se}_512_u8", _time_ms(f, flush, 20, 5), x.numel(), 2 * x.numel())
+
+    def cfg2_4096():
+        f = synthetic.smoothed_noise_u8((4096, 4096), 1, 4.0)
+        x = torch.from_numpy(f).to(dev)
+        o = torch.empty_like(x)
+        ms = _time_ms(lambda: geo.h_maxima_binary(x, H_VALUE, Common_NL_SE.SESquare2D, o, check=False), flush, 5, 2)
+        cpu_v, kind, runs = cpu_hmaxima(f, budget_s=0.0)
+        cpu_ms = f.size / cpu_v * 1e3
+        rec("cfg2_h_maxima_binary_4096_u8", ms, f.size, 2 * f.size, cpu_ms=cpu_ms, cpu_kind=kind,
+            speedup_vs_cpu=cpu_ms / ms, rounds=geo.last_reconstruction_rounds())
+
+    def cfg2_leveling():
+        f = synthetic.smoothed_noise_u8((2048, 2048), 1, 4.0)
+        m = synthetic.leveling_marker(f, 16.0)
+        x, mk = torch.from_numpy(f).to(dev), torch.from_numpy(m).to(dev)
+        o = torch.empty_like(x)
+        ms = _time_ms(lambda: geo.leveling(x, mk, Common_NL_SE.SESquare2D, o, check=False), flush, 5, 2)
+        kw = {}
+        try:
+            from oracle import ref
+            if ref.available():
+                t0 = time.perf_counter()
+                ref.leveling("leveling", f, m, "SESquare2D")
+                kw = {"cpu_ms": (time.perf_counter() - t0) * 1e3, "cpu_kind": "reference"}
+                kw["speedup_vs_cpu"] = kw["cpu_ms"] / ms
+        except Exception:
+            pass
+        rec("cfg2_leveling_2048_u8", ms, f.size, 3 * f.size, **kw)
+
+    def cfg3():
+        for dt, arr in (("u16", synthetic.uniform_u16((4096, 4096), 2)), ("f32", synthetic.normal_f32((4096, 4096), 3))):
+            x = torch.from_numpy(arr).to(dev)
+            o = torch.empty_like(x)
+            es = x.element_size()
+            for sname, se in (("square31", llm.se_rect(15, 15)), ("h63", llm.se_line(0, 1, 31)),
+                              ("v63", llm.se_line(1, 0, 31)), ("d45_63", llm.se_line(-1, 1, 31))):
+                for op, fn in (("dilate", llm.DilateSE), ("erode", llm.ErodeSE), ("opening", llm.Opening),
+                               ("closing", llm.Closing), ("gradient", llm.Gradient)):
+                    ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 5, 2)
+                    rec(f"cfg3_{op}_{sname}_4096_{dt}", ms, x.numel(), 2 * x.numel() * es)
+            del x, o
+        v = torch.from_numpy(synthetic.uniform_u8((256, 256, 256), 4)).to(dev)
+        o = torch.empty_like(v)
+        for dil in (True, False):
+            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(v, Common_NL_SE.SESquare3D, 1, o), flush, 10, 3)
+            rec(f"cfg3_{'dilate' if dil else 'erode'}_cube3_256_u8", ms, v.numel(), 2 * v.numel())
+
+    def cfg4():
+        imgs = synthetic.ragged_batch(512, 5, 4.0)
+        xs = [torch.from_numpy(f).to(dev) for f in imgs]
+        outs = [torch.empty_like(x) for x in xs]
+        npx = sum(f.size for f in imgs)
+        batch_ms = _time_ms(lambda: geo.h_maxima_binary_batch(xs, 10, Common_NL_SE.SESquare2D, outs, check=False),
+                            flush, 5, 2)
+
+        def plain():
+            for x, o in zip(xs, outs):
+                geo.h_maxima_binary(x, 10, Common_NL_SE.SESquare2D, o, check=False)
+        plain_ms = _time_ms(plain, flush, 3, 1)
+        rec("cfg4_ragged512_batch_one_launch", batch_ms, npx, 2 * npx, plain_ms=plain_ms,
+            speedup_vs_plain=plain_ms / batch_ms)
+
+    def cfg5():
+        shape = (64, 32, 256, 256)
+        x = torch.randn(shape, device=dev, generator=torch.Generator(device=dev).manual_seed(6))
+        g = torch.randn(shape, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
+        n = x.numel()
+        for name, fn in (("dilation", autograd.dilation), ("erosion", autograd.erosion), ("opening", autograd.opening)):
+            with torch.no_grad():
+                fwd = _time_ms(lambda fn=fn: fn(x, 2), flush, 3, 1)
+            xr = x.clone().requires_grad_(True)
+
+            def fb(fn=fn):
+                xr.grad = None
+                fn(xr, 2).backward(g)
+            fb_ms = _time_ms(fb, flush, 3, 1)
+            passes = 2 if name == "opening" else 1
+            rec(f"cfg5_{name}_5x5_fwd_64x32x256x256_f32", fwd, n, passes * 2 * n * 4)
+            rec(f"cfg5_{name}_5x5_fwd_bwd_64x32x256x256_f32", fb_ms, n, passes * 5 * n * 4, fwd_bwd_over_fwd=fb_ms / fwd)
+            del xr
+
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5):
+        guard(fn)
+    return res
 
 
 def flush_l2(buf):
@@ -284,11 +416,12 @@ def run_gpu(args):
         "gpu_launches": args.steps,  # one persistent k_reconstruct launch per step (plus one memset)
         "clocks": clocks,
     }
-    if rank == 0 and not args.no_cpu:
-        v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
-        line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
-                                "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
-                                          f"(poutre2 is single-threaded)"}
+    if rank == 0:
+        if not args.no_cpu:
+            v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
+            line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
+                                    "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
+                                              f"(poutre2 is single-threaded)"}
         if args.extra:
             line["extra"] = extra_measurements(dev, flush)
         print(json.dumps(line))
@@ -305,7 +438,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--extra", action="store_true", help="also measure the other workloads")
+    ap.add_argument("--extra", action="store_true", default=True, help="also measure the other workloads (default)")
+    ap.add_argument("--no-extra", dest="extra", action="store_false")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
