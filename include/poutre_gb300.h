@@ -201,6 +201,25 @@ PG_API pg_status pg_flat_morph2d_forward(const float *x, float *y, int64_t plane
 PG_API pg_status pg_flat_morph2d_backward(const float *x, const float *grad_out, float *grad_in, int64_t planes, int64_t h,
                                    int64_t w, int32_t ry, int32_t rx, int32_t dilate, pg_stream_t stream);
 
+/* Size of the fixed device scratch of pg_reconstruction_noalloc (1 MiB). */
+#define PG_NOALLOC_SCRATCH_BYTES (1u << 20)
+
+/* Geodesic reconstruction that allocates no device memory.  No counterpart in the reference:
+ * it exists for callers that cannot allocate -- e.g. a real-time imaging pipeline that
+ * reserves all of its device memory up front and forbids cudaMalloc in steady state (an
+ * allocation may synchronise the device or fail under memory pressure), or a host that gives
+ * this library a fixed memory budget.  Same arguments, checks and result as
+ * pg_reconstruction (1D and 2D SEs); the caller still provides marker, mask and output.
+ * Its scratch (control block + tile worklist) is a 1 MiB file-scope device array that every
+ * GPU loading the library holds until exit, so the image may span at most 131040 tiles
+ * (64x64 pixels; 32x32 for 8-byte pixels) -- about 536 Mpixel for 1..4-byte pixels -- and
+ * larger images are rejected with PG_ERR_INVALID_ARGUMENT.  All calls share that array: calls
+ * that overlap on the GPU (other streams, other threads) race and must be serialised by the
+ * caller.  The first call on a device looks the array's address up; make it before any
+ * stream capture.  Device-side failure is reported by pg_check_device, as for the others. */
+PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const pg_image *mask,
+                                           int32_t common_se, const pg_image *out, pg_stream_t stream);
+
 /* Synchronises `stream`, then returns (and clears) the device-side status of the geodesy
  * kernels: PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device
  * wait) since the last check, else PG_OK.  The geodesy calls above are asynchronous; call this

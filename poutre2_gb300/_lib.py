@@ -30,7 +30,7 @@ EXPORTED = [
     "pg_low_leveling", "pg_high_leveling", "pg_leveling",
     "pg_sat_sub_constant", "pg_sat_add_constant",
     "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
-    "pg_check_device", "pg_last_reconstruction_rounds",
+    "pg_check_device", "pg_last_reconstruction_rounds", "pg_reconstruction_noalloc",
 ]
 
 
@@ -92,6 +92,7 @@ def load(path: str | None = None):
             "pg_flat_morph2d_forward": [fp, fp, I64, I64, I64, I32, I32, I32, VP],
             "pg_flat_morph2d_backward": [fp, fp, fp, I64, I64, I64, I32, I32, I32, VP],
             "pg_check_device": [VP],
+            "pg_reconstruction_noalloc": [I32, img, img, I32, img, VP],
         }
         for name, args in sig.items():
             f = getattr(L, name)

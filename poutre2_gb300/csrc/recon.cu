@@ -510,6 +510,103 @@ pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, 
   return PG_OK;
 }
 
+// ------------------------------------------------------------------ allocation-free variant
+// For callers that must not touch the device allocator (see pg_reconstruction_noalloc in
+// include/poutre_gb300.h).  Its only scratch -- the control block and the tile worklist --
+// lives in this file-scope array, which every GPU that loads the library holds until exit.
+static constexpr size_t kNoAllocScratchBytes = PG_NOALLOC_SCRATCH_BYTES;
+static constexpr size_t kNoAllocFlagsOffset = 256;  // RCtl fits below
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static_assert(sizeof(RCtl) <= kNoAllocFlagsOffset, "control block must fit below the flags");
+
+// Device address of g_noalloc_scratch, looked up once per device with that device current.
+// In host code the symbol name is only a host-side stand-in, so the kernel is given this
+// address instead.
+static pg_status noalloc_scratch(void **out) {
+  static std::mutex mu;
+  static std::vector<void *> addr;  // indexed by device ordinal
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  if ((size_t)dev >= addr.size()) addr.resize((size_t)dev + 1, nullptr);
+  if (!addr[(size_t)dev]) {
+    void *p = nullptr;
+    PG_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+    addr[(size_t)dev] = p;
+  }
+  *out = addr[(size_t)dev];
+  return PG_OK;
+}
+
+template <typename T, bool SUP, bool CONN8>
+static pg_status run_noalloc_t(RImg im, cudaStream_t s) {
+  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  im.tiles_x = (int)ceil_div(im.W, RT);
+  im.tiles_y = (int)ceil_div(im.H, RT);
+  im.tile_begin = 0;
+  const int64_t ntiles = (int64_t)im.tiles_x * im.tiles_y;
+  if (ntiles == 0) return PG_OK;
+  const int64_t max_tiles = (int64_t)((kNoAllocScratchBytes - kNoAllocFlagsOffset) / (2 * sizeof(unsigned)));
+  if (ntiles > max_tiles)
+    return fail(PG_ERR_INVALID_ARGUMENT, "pg_reconstruction_noalloc: the image needs " + std::to_string(ntiles) +
+                                             " tiles of " + std::to_string(RT) + "x" + std::to_string(RT) +
+                                             " pixels; the fixed scratch holds at most " + std::to_string(max_tiles));
+  void *base = nullptr;
+  PG_TRY(noalloc_scratch(&base));
+  // the control block and both flag buffers must start at zero; the array keeps the
+  // previous call's contents
+  const size_t used = kNoAllocFlagsOffset + 2 * sizeof(unsigned) * (size_t)ntiles;
+  PG_CUDA_TRY(cudaMemsetAsync(base, 0, used, s), "clear no-alloc scratch");
+  RParams<T> P{};
+  P.single = im;
+  P.imgs = nullptr;
+  P.nimg = 1;
+  P.ntiles = (int)ntiles;
+  P.ctl = static_cast<RCtl *>(base);
+  P.flags = reinterpret_cast<unsigned *>(static_cast<char *>(base) + kNoAllocFlagsOffset);
+  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * ntiles);
+  P.init = INIT_MARKER;
+  P.mask_mode = MASK_PLAIN;
+  P.epi = EPI_NONE;
+  P.h = static_cast<T>(0);
+  auto kern = k_reconstruct<T, SUP, CONN8>;
+  int per_sm = 0;
+  PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RTHREADS, 0), "occupancy");
+  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
+  int64_t grid = (int64_t)per_sm * num_sms();
+  if (grid > ntiles) grid = ntiles;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(RTHREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P), "cooperative reconstruction launch (no-alloc)");
+  return PG_OK;
+}
+
+static pg_status reconstruction_noalloc(bool dilate, bool conn8, const pg_image &marker, const pg_image &mask,
+                                        const pg_image &out, cudaStream_t s) {
+  const Dims d = dims_of(mask);
+  RImg im{};
+  im.marker = marker.data;
+  im.mask = mask.data;
+  im.rec = out.data;
+  im.out = out.data;
+  im.H = d.nz * d.ny;
+  im.W = d.nx;
+  PG_DISPATCH_PTYPE(mask.ptype, T, {
+    if (dilate) return conn8 ? run_noalloc_t<T, true, true>(im, s) : run_noalloc_t<T, true, false>(im, s);
+    return conn8 ? run_noalloc_t<T, false, true>(im, s) : run_noalloc_t<T, false, false>(im, s);
+  });
+  return PG_OK;
+}
+
 }  // namespace pg
 
 extern "C" {
@@ -532,6 +629,58 @@ int32_t pg_last_reconstruction_rounds(void) {
   if (cudaDeviceSynchronize() != cudaSuccess) return -1;
   if (cudaMemcpyFromSymbol(&r, pg::g_recon_rounds, sizeof(int)) != cudaSuccess) return -1;
   return r;
+}
+
+// Reconstruction that allocates nothing: same checks and result as pg_reconstruction, scratch
+// taken from g_noalloc_scratch.  The first call on a device looks up that array's device
+// address; make it before any stream capture.
+pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const pg_image *mask, int32_t se,
+                                    const pg_image *out, pg_stream_t stream) {
+  auto chk = [](const pg_image *a, const pg_image *b) -> pg_status {
+    if (!a || !b) return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_Reconstruct: null image descriptor");
+    if (a->rank < 1 || a->rank > 3 || b->rank != a->rank)
+      return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible size");
+    for (int i = 0; i < a->rank; ++i)
+      if (a->shape[i] != b->shape[i] || a->shape[i] < 0) return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible size");
+    if (!pg::elem_size(a->ptype)) return pg::fail(PG_ERR_UNSUPPORTED_PTYPE, "unsupported PTYPE");
+    if (a->ptype != b->ptype) return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible types");
+    const int64_t n = pg::dims_of(*a).count();
+    if (n > 0 && (!a->data || !b->data)) return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_Reconstruct: null data pointer");
+    return PG_OK;
+  };
+  auto distinct = [](const pg_image *a, const pg_image *b) -> pg_status {
+    const int64_t n = pg::dims_of(*a).count();
+    const size_t bytes = (size_t)n * pg::elem_size(a->ptype);
+    const char *pa = static_cast<const char *>(a->data), *pb = static_cast<const char *>(b->data);
+    if (n > 0 && pa < pb + bytes && pb < pa + bytes)
+      return pg::fail(PG_ERR_ALIASING, "t_Reconstruct output must be != than input images");
+    return PG_OK;
+  };
+  PG_TRY(chk(marker, out));
+  PG_TRY(chk(mask, out));
+  {
+    // size limit of the fixed scratch, checked on the shape alone
+    const pg::Dims d = pg::dims_of(*mask);
+    const int rt = pg::elem_size(mask->ptype) == 8 ? 32 : 64;
+    const int64_t ntiles = pg::ceil_div(d.nz * d.ny, rt) * pg::ceil_div(d.nx, rt);
+    const int64_t max_tiles = (int64_t)((pg::kNoAllocScratchBytes - pg::kNoAllocFlagsOffset) / (2 * sizeof(unsigned)));
+    if (ntiles > max_tiles)
+      return pg::fail(PG_ERR_INVALID_ARGUMENT, "pg_reconstruction_noalloc: the image needs " + std::to_string(ntiles) +
+                                                   " tiles; the fixed scratch holds at most " +
+                                                   std::to_string(max_tiles));
+  }
+  PG_TRY(distinct(marker, out));
+  PG_TRY(distinct(mask, out));
+  if (type != PG_RECONSTRUCT_ERODE && type != PG_RECONSTRUCT_DILATE)
+    return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_ReconstructionDispatchRectType unsupported reconstruction_type");
+  bool conn8 = true;
+  const int rank = mask->rank;
+  if (rank == 1 && se == PG_SE_SEGMENT_X_1D) conn8 = true;
+  else if (rank == 2 && se == PG_SE_SQUARE_2D) conn8 = true;
+  else if (rank == 2 && se == PG_SE_CROSS_2D) conn8 = false;
+  else return pg::fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
+  return pg::reconstruction_noalloc(type == PG_RECONSTRUCT_DILATE, conn8, *marker, *mask, *out,
+                                    reinterpret_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"
