@@ -97,6 +97,46 @@ template <typename T> struct Pack {
   }
 };
 
+// Two adjacent packs (32 bytes): twice the bytes in flight per thread, same interface.
+template <typename T> struct Pack2 {
+  static constexpr int N = 2 * Pack<T>::N;
+  Pack<T> a, b;
+  __device__ __forceinline__ static Pack2 load(const T *p) {
+    Pack2 r;
+    r.a = Pack<T>::load(p);
+    r.b = Pack<T>::load(p + Pack<T>::N);
+    return r;
+  }
+  __device__ __forceinline__ void store(T *p) const {
+    a.store(p);
+    b.store(p + Pack<T>::N);
+  }
+  __device__ __forceinline__ static Pack2 fill(T x) {
+    Pack2 r;
+    r.a = Pack<T>::fill(x);
+    r.b = r.a;
+    return r;
+  }
+  template <bool SUP> __device__ __forceinline__ static Pack2 op(const Pack2 &x, const Pack2 &y) {
+    Pack2 r;
+    r.a = Pack<T>::template op<SUP>(x.a, y.a);
+    r.b = Pack<T>::template op<SUP>(x.b, y.b);
+    return r;
+  }
+  __device__ __forceinline__ Pack2 shl(T left) const {
+    Pack2 r;
+    r.a = a.shl(left);
+    r.b = b.shl(a.last());
+    return r;
+  }
+  __device__ __forceinline__ Pack2 shr(T right) const {
+    Pack2 r;
+    r.a = a.shr(b.first());
+    r.b = b.shr(right);
+    return r;
+  }
+};
+
 // ------------------------------------------------------------------ host-side plumbing
 void set_error(const std::string &msg);
 pg_status fail(pg_status st, const std::string &msg);
@@ -180,6 +220,10 @@ inline Dims dims_of(const pg_image &im) {
 pg_status launch_small_se(const pg_image &in, const pg_image &out, int se, bool dilate, cudaStream_t s);
 pg_status launch_nl(const pg_image &in, const pg_image &out, const int32_t *offsets, int n, bool dilate, cudaStream_t s);
 pg_status launch_line(const pg_image &in, const pg_image &out, int dy, int dx, int64_t half, bool dilate, cudaStream_t s);
+bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
+                     pg_status *st);
+bool try_line_words(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
+                    pg_status *st);
 pg_status launch_rect(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s);
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);

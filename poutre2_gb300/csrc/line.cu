@@ -186,6 +186,17 @@ pg_status launch_line(const pg_image &in, const pg_image &out, int dy, int dx, i
   if (!((dy == 0 && dx == 1) || (dy == 1 && (dx == 0 || dx == 1 || dx == -1))))
     return fail(PG_ERR_UNSUPPORTED_SE, "line direction must be X, Y or a 45-degree diagonal");
   if (half < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative half segment");
+  // clipping makes any half length beyond the image's reach equivalent to that reach
+  int64_t kmax;
+  if (dy == 0) kmax = d.nx - 1;
+  else if (dx == 0) kmax = d.ny - 1;
+  else kmax = std::min(d.ny, d.nx) - 1;
+  const int64_t k = std::min<int64_t>(half, std::max<int64_t>(kmax, 0));
+  if (k >= 1 && k <= (1 << 20)) {
+    pg_status st = PG_OK;
+    if (try_line_stream(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
+    if (try_line_words(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
+  }
   PG_DISPATCH_PTYPE(in.ptype, T, {
     const T *src = static_cast<const T *>(in.data);
     T *dst = static_cast<T *>(out.data);

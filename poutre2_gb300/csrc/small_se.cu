@@ -83,16 +83,20 @@ __global__ void __launch_bounds__(256) k_small3d(const T *__restrict__ in, T *__
   const int64_t x0 = xp * P::N;
   const int64_t z1 = (z0 + R < D) ? z0 + R : D;
   const T NEU = Op<T, SUP>::neutral();
+  const int64_t plane = H * W;
+  const bool has_up = y >= 1, has_dn = y + 1 < H;
+  // row pointers of this thread's (y-1, y, y+1) rows in slice z, advanced by one plane per slice
+  const T *row_m = in + y * W;
   auto slice = [&](int64_t z, P &A, P &B) {
     if (z < 0 || z >= D) { A = P::fill(NEU); B = A; return; }
-    const T *base = in + z * H * W;
+    const T *rm = row_m + z * plane;
     P cu, hu, cm, hm, cd, hd;
     const bool need_rows = (SHAPE == SH_SQUARE || SHAPE == SH_CROSS || SHAPE == SH_SEGY);
     const bool need_h = (SHAPE != SH_SEGY && SHAPE != SH_SEGZ);
-    load_row<T, SUP>(base + y * W, true, x0, W, need_h, cm, hm);
+    load_row<T, SUP>(rm, true, x0, W, need_h, cm, hm);
     if (need_rows) {
-      load_row<T, SUP>(base + (y - 1) * W, y >= 1, x0, W, SHAPE == SH_SQUARE, cu, hu);
-      load_row<T, SUP>(base + (y + 1) * W, y + 1 < H, x0, W, SHAPE == SH_SQUARE, cd, hd);
+      load_row<T, SUP>(rm - W, has_up, x0, W, SHAPE == SH_SQUARE, cu, hu);
+      load_row<T, SUP>(rm + W, has_dn, x0, W, SHAPE == SH_SQUARE, cd, hd);
     }
     if constexpr (SHAPE == SH_SQUARE) { A = P::template op<SUP>(P::template op<SUP>(hu, hm), hd); B = A; }
     else if constexpr (SHAPE == SH_CROSS) { A = P::template op<SUP>(P::template op<SUP>(cu, hm), cd); B = cm; }
@@ -141,26 +145,35 @@ static int rows_per_thread(int64_t threads_without_strips, int64_t length, int c
 
 template <typename T, bool SUP, int SHAPE>
 static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream_t s) {
-  const bool vec = (W % Pack<T>::N == 0) && ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const bool vec2 = false;  // two packs per thread measured slower than one
+  const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
   const int R = rows_per_thread(npack, H, 32);
-  dim3 block(32, 8);
-  dim3 grid((unsigned)ceil_div(npack, 32), (unsigned)ceil_div(ceil_div(H, R), 8));
+  const int bx = npack >= 32 ? 32 : npack >= 16 ? 16 : npack >= 8 ? 8 : npack >= 4 ? 4 : npack >= 2 ? 2 : 1;
+  dim3 block(bx, 256 / bx);
+  dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(ceil_div(H, R), 256 / bx));
   if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the small-SE kernel");
-  if (vec) k_small2d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  if (vec2) k_small2d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  else if (vec) k_small2d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   else k_small2d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 2D kernel launch");
 }
 
 template <typename T, bool SUP, int SHAPE>
 static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W, cudaStream_t s) {
-  const bool vec = (W % Pack<T>::N == 0) && ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
+  const bool vec2 = false;  // two packs per thread measured slower than one
+  const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
   const int R = rows_per_thread(npack * H, D, 16);
-  dim3 block(32, 8);
-  dim3 grid((unsigned)ceil_div(npack, 32), (unsigned)ceil_div(H, 8), (unsigned)ceil_div(D, R));
+  // no idle lanes when a row holds fewer than 32 packs
+  const int bx = npack >= 32 ? 32 : npack >= 16 ? 16 : npack >= 8 ? 8 : npack >= 4 ? 4 : npack >= 2 ? 2 : 1;
+  dim3 block(bx, 256 / bx);
+  dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(H, 256 / bx), (unsigned)ceil_div(D, R));
   if (grid.y > 65535 || grid.z > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "volume too large for the small-SE kernel");
-  if (vec) k_small3d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  if (vec2) k_small3d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  else if (vec) k_small3d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   else k_small3d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 3D kernel launch");
 }

@@ -173,7 +173,7 @@ def test_neighbor_list(dt):
 def test_lines_xy(dt, half):
     from poutre2_gb300 import llm
     rng = np.random.default_rng(half)
-    for shape in [(1, 300), (37, 37), (130, 130)]:
+    for shape in [(1, 300), (37, 37), (130, 130), (132, 132), (257, 256)]:
         a = rand(rng, shape, dt)
         x = dev(a)
         for name, axis in (("X", "x"), ("Y", "y")):
@@ -185,20 +185,22 @@ def test_lines_xy(dt, half):
                 np.testing.assert_array_equal(host(out), oracle.line(a, half, axis, dil), err_msg=f"{name} {shape}")
 
 
-@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.float32, np.float64])
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32, np.float64])
 @pytest.mark.parametrize("d", [(0, 1), (1, 0), (-1, 1), (1, 1)])
 @pytest.mark.parametrize("half", [1, 5, 31])
 def test_segments_any_direction(dt, d, half):
     from poutre2_gb300 import llm
     from poutre2_gb300.se import NeighborList
     rng = np.random.default_rng(half * 7 + d[0] * 3 + d[1])
-    a = rand(rng, (77, 150), dt)
-    x = dev(a)
     offs = NeighborList.segment(d[0], d[1], half).offsets
-    for dil in (True, False):
-        out = torch.empty_like(x)
-        (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_line(d[0], d[1], half), out)
-        np.testing.assert_array_equal(host(out), oracle.erode_dilate_nl(a, offs, dil))
+    # word-aligned rows for every pixel type (fast path) and a ragged width (fallback)
+    for shape in [(77, 150), (100, 136), (9, 260), (200, 64), (3, 4)]:
+        a = rand(rng, shape, dt)
+        x = dev(a)
+        for dil in (True, False):
+            out = torch.empty_like(x)
+            (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_line(d[0], d[1], half), out)
+            np.testing.assert_array_equal(host(out), oracle.erode_dilate_nl(a, offs, dil), err_msg=f"{shape}")
 
 
 @pytest.mark.parametrize("dt", [np.uint16, np.float32])
