@@ -277,15 +277,28 @@ def extra_measurements(dev, flush):
         xs = [torch.from_numpy(f).to(dev) for f in imgs]
         outs = [torch.empty_like(x) for x in xs]
         npx = sum(f.size for f in imgs)
-        batch_ms = _time_ms(lambda: geo.h_maxima_binary_batch(xs, 10, Common_NL_SE.SESquare2D, outs, check=False),
-                            flush, 5, 2)
+        plan = geo.HMaximaBinaryBatch(xs, 10, Common_NL_SE.SESquare2D, outs, autotune=True)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            plan.run()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            plan.run()
+        graph_ms = _time_ms(graph.replay, flush, 5, 2)
+        plan_ms = _time_ms(plan.run, flush, 5, 2)
+        one_call_ms = _time_ms(lambda: geo.h_maxima_binary_batch(xs, 10, Common_NL_SE.SESquare2D, outs, check=False),
+                               flush, 5, 2)
 
         def plain():
             for x, o in zip(xs, outs):
                 geo.h_maxima_binary(x, 10, Common_NL_SE.SESquare2D, o, check=False)
         plain_ms = _time_ms(plain, flush, 3, 1)
-        rec("cfg4_ragged512_batch_one_launch", batch_ms, npx, 2 * npx, plain_ms=plain_ms,
-            speedup_vs_plain=plain_ms / batch_ms)
+        rec("cfg4_ragged512_graph_replay", graph_ms, npx, 2 * npx, plain_ms=plain_ms,
+            speedup_vs_plain=plain_ms / graph_ms, plan_run_ms=plan_ms, one_call_ms=one_call_ms,
+            autotuned=plan.config)
+        plan.close()
 
     def cfg5():
         shape = (64, 32, 256, 256)

@@ -173,6 +173,21 @@ PG_API pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t common
 PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t common_se,
                                    pg_stream_t stream);
 
+/* A prepared ragged batch of the binary h-maxima (no reference counterpart): the image and tile
+ * tables, the worklist and the reconstruction buffers stay on the device, so a run is one
+ * memset plus one persistent cooperative launch, both of which can be captured in a CUDA graph.
+ * With autotune != 0 the plan times tile side (64 or 32 pixels = threads per tile) x sweep sets
+ * per tile visit (4, 16, unbounded) on this batch and keeps the fastest; the choice is cached per
+ * (pixel type, connectivity, batch size class).  Inputs/outputs must stay valid while the plan
+ * is used.  Plan creation synchronises the device. */
+typedef struct pg_batch_plan pg_batch_plan;
+PG_API pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, double h,
+                                               int32_t common_se, int32_t autotune, pg_batch_plan **plan,
+                                               pg_stream_t stream);
+PG_API pg_status pg_batch_plan_run(pg_batch_plan *plan, pg_stream_t stream);
+PG_API pg_status pg_batch_plan_config(const pg_batch_plan *plan, int32_t *tile, int32_t *sweeps, int32_t *grid);
+PG_API pg_status pg_batch_plan_destroy(pg_batch_plan *plan);
+
 /* poutre::geo::low_leveling / high_leveling / leveling(const IInterface& ref, const IInterface& marker,
  * se::Common_NL_SE, IInterface&), include/poutre/geodesy/leveling.hpp:37-52. */
 PG_API pg_status pg_low_leveling(const pg_image *ref, const pg_image *marker, int32_t common_se, const pg_image *out,

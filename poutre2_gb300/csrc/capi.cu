@@ -425,6 +425,31 @@ pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, in
   return launch_reconstruction(nullptr, ins, outs, n, rq, STREAM(s));
 }
 
+pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t se,
+                                        int32_t autotune, pg_batch_plan **plan, pg_stream_t s) {
+  if (!plan) return fail(PG_ERR_INVALID_ARGUMENT, "null plan pointer");
+  *plan = nullptr;
+  if (n < 1 || !ins || !outs) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch_plan: bad image arrays");
+  for (int i = 0; i < n; ++i) {
+    PG_TRY(check_binary_out(&ins[i], &outs[i], "h_maxima_binary_batch_plan"));
+    if (ins[i].ptype != ins[0].ptype || ins[i].rank != ins[0].rank)
+      return fail(PG_ERR_INCOMPATIBLE, "h_maxima_binary_batch_plan: all images must share pixel type and rank");
+    if (dims_of(ins[i]).count() == 0) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch_plan: empty image");
+  }
+  PG_TRY(check_scalar(ins[0].ptype, h, "h_maxima_binary_batch_plan"));
+  bool conn8 = true;
+  PG_TRY(recon_se(se, ins[0].rank, conn8));
+  return create_batch_plan(ins, outs, n, h, conn8, autotune != 0, STREAM(s), plan);
+}
+pg_status pg_batch_plan_run(pg_batch_plan *plan, pg_stream_t s) {
+  if (!plan) return fail(PG_ERR_INVALID_ARGUMENT, "null plan");
+  return run_batch_plan(plan, STREAM(s));
+}
+pg_status pg_batch_plan_destroy(pg_batch_plan *plan) {
+  destroy_batch_plan(plan);
+  return PG_OK;
+}
+
 static pg_status leveling_half(const pg_image *ref, const pg_image *marker, int se, const pg_image *out, bool low,
                                cudaStream_t s) {
   ReconRequest rq;

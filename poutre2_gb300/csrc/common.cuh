@@ -247,6 +247,11 @@ struct ReconRequest {
 pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
                                 const ReconRequest &rq, cudaStream_t s);
 
+pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, double h, bool conn8, bool autotune,
+                            cudaStream_t s, pg_batch_plan **out_plan);
+pg_status run_batch_plan(pg_batch_plan *p, cudaStream_t s);
+void destroy_batch_plan(pg_batch_plan *p);
+
 pg_status launch_flat2d(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int ry, int rx, bool dilate,
                         cudaStream_t s);
 pg_status launch_flat2d_backward(const float *x, const float *gy, float *gx, int64_t planes, int64_t h, int64_t w,

@@ -27,7 +27,11 @@
 //    loop after max_rounds, recording PG_ERR_NOT_CONVERGED in a device status word.
 #include <algorithm>
 #include <atomic>
+#include <cmath>
+#include <map>
+#include <memory>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -73,6 +77,7 @@ template <typename T> struct RParams {
   RCtl *ctl;
   unsigned *flags;    // 2 * ntiles
   int max_rounds;
+  int max_sweeps = kMaxSweeps;  // sweep sets per tile visit before the tile yields (and re-flags itself)
   int init, mask_mode, epi;
   T h;
 };
@@ -184,10 +189,10 @@ template <typename T> __device__ __forceinline__ void st_cg(T *p, T v) {
 
 enum : int { B_N = 1, B_S = 2, B_W = 4, B_E = 8, B_NW = 16, B_NE = 32, B_SW = 64, B_SE = 128, B_SELF = 256 };
 
-template <typename T, bool SUP, bool CONN8>
+template <typename T, bool SUP, bool CONN8, int RT>
 __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, int round, T *s_out, T *s_mask,
                              int *s_flag) {
-  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  constexpr int RTHREADS = RT;
   constexpr int PO = tile_pitch<T>(RT + 2);
   constexpr int PM = tile_pitch<T>(RT);
   const T NEU = Op<T, SUP>::neutral();
@@ -238,7 +243,7 @@ __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, i
     return false;
   };
   const int lane = threadIdx.x;  // column for vertical sweeps, row for horizontal ones
-  for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+  for (int sweep = 0; sweep < P.max_sweeps; ++sweep) {
     bool ch = false;
     // down: neighbours in the row above
     for (int r = 0; r < RT; ++r) {
@@ -329,9 +334,9 @@ __device__ __forceinline__ const RImg &image_of(const RParams<T> &P, int tile, i
   return P.imgs[lo];
 }
 
-template <typename T, bool SUP, bool CONN8>
-__global__ void __launch_bounds__(tile_side<T>()) k_reconstruct(RParams<T> P) {
-  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+template <typename T, bool SUP, bool CONN8, int RT = tile_side<T>()>
+__global__ void __launch_bounds__(RT) k_reconstruct(RParams<T> P) {
+  constexpr int RTHREADS = RT;
   constexpr int PO = tile_pitch<T>(RT + 2);
   constexpr int PM = tile_pitch<T>(RT);
   __shared__ __align__(16) T s_out[(RT + 2) * PO];
@@ -360,7 +365,7 @@ __global__ void __launch_bounds__(tile_side<T>()) k_reconstruct(RParams<T> P) {
       if (active) {
         int tl = 0;
         const RImg &im = image_of(P, t, tl);
-        process_tile<T, SUP, CONN8>(im, P, tl, round, s_out, s_mask, &s_flag);
+        process_tile<T, SUP, CONN8, RT>(im, P, tl, round, s_out, s_mask, &s_flag);
       }
     }
     if (!grid_barrier(ctl)) { ok = false; break; }
@@ -508,6 +513,224 @@ pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, 
   }
   PG_DISPATCH_PTYPE(masks[0].ptype, T, { return run_dispatch<T>(imgs, rq, s); });
   return PG_OK;
+}
+
+// ------------------------------------------------------------------ batch plans + autotuner
+// A plan keeps a ragged batch's image tables, worklist and reconstruction buffers on the device
+// so that each run is one memset and one cooperative launch (both capturable in a CUDA graph).
+// The autotuner times the candidate configurations -- tile side (64 or 32 pixels, i.e. 64 or
+// 32 threads per tile) x sweep sets per tile visit before the tile yields to the next global
+// round (4, 16, unbounded) -- on the plan's own batch and keeps the fastest; the choice is
+// cached per (pixel type, connectivity, batch size class).
+struct PlanCfg {
+  int rt = 64;
+  int sweeps = kMaxSweeps;
+};
+
+struct PlanTable {  // one tile decomposition of the batch
+  int ntiles = 0;
+  RImg *d_imgs = nullptr;  // device table
+  std::vector<RImg> imgs;  // host copy
+};
+
+}  // namespace pg
+
+struct pg_batch_plan {
+  int device = 0;
+  int ptype = 0;
+  bool conn8 = true;
+  double h = 0;
+  void *scratch = nullptr;  // control block | flags (sized for the finest tiling) | recon buffers
+  size_t clear_bytes = 0;
+  pg::PlanTable t64, t32;
+  pg::PlanCfg cfg;
+  int grid = 0;
+};
+
+namespace pg {
+
+template <int RT> static PlanTable &plan_table(pg_batch_plan &p) { return RT == 64 ? p.t64 : p.t32; }
+
+template <typename T, bool CONN8, int RT>
+static pg_status plan_launch_t(pg_batch_plan &p, int sweeps, cudaStream_t s, int *grid_out) {
+  PlanTable &tb = plan_table<RT>(p);
+  RParams<T> P{};
+  P.single = tb.imgs[0];
+  P.imgs = tb.d_imgs;
+  P.nimg = (int)tb.imgs.size();
+  P.ntiles = tb.ntiles;
+  P.ctl = static_cast<RCtl *>(p.scratch);
+  P.flags = reinterpret_cast<unsigned *>(static_cast<char *>(p.scratch) + 256);
+  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)tb.ntiles);
+  P.max_sweeps = sweeps;
+  P.init = INIT_SAT_CONST;
+  P.mask_mode = MASK_PLAIN;
+  P.epi = EPI_BINARY_SUP;
+  P.h = static_cast<T>(p.h);
+  auto kern = k_reconstruct<T, true, CONN8, RT>;
+  int per_sm = 0;
+  PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RT, 0), "occupancy");
+  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
+  int grid = per_sm * num_sms();
+  if (grid > tb.ntiles) grid = tb.ntiles;
+  if (grid_out) *grid_out = grid;
+  PG_CUDA_TRY(cudaMemsetAsync(p.scratch, 0, p.clear_bytes, s), "clear batch worklist");
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(RT);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P), "cooperative batch launch");
+  return PG_OK;
+}
+
+template <typename T>
+static pg_status plan_launch(pg_batch_plan &p, const PlanCfg &c, cudaStream_t s, int *grid_out) {
+  if constexpr (sizeof(T) == 8) {
+    return p.conn8 ? plan_launch_t<T, true, 32>(p, c.sweeps, s, grid_out) : plan_launch_t<T, false, 32>(p, c.sweeps, s, grid_out);
+  } else {
+    if (c.rt == 64)
+      return p.conn8 ? plan_launch_t<T, true, 64>(p, c.sweeps, s, grid_out) : plan_launch_t<T, false, 64>(p, c.sweeps, s, grid_out);
+    return p.conn8 ? plan_launch_t<T, true, 32>(p, c.sweeps, s, grid_out) : plan_launch_t<T, false, 32>(p, c.sweeps, s, grid_out);
+  }
+}
+
+static pg_status plan_run(pg_batch_plan &p, const PlanCfg &c, cudaStream_t s, int *grid_out) {
+  PG_DISPATCH_PTYPE(p.ptype, T, { return plan_launch<T>(p, c, s, grid_out); });
+  return PG_OK;
+}
+
+static void plan_tables(pg_batch_plan &p, const std::vector<RImg> &base, int rt, PlanTable &tb) {
+  tb.imgs = base;
+  int ntiles = 0;
+  for (auto &im : tb.imgs) {
+    im.tiles_x = (int)ceil_div(im.W, rt);
+    im.tiles_y = (int)ceil_div(im.H, rt);
+    im.tile_begin = ntiles;
+    ntiles += im.tiles_x * im.tiles_y;
+  }
+  tb.ntiles = ntiles;
+}
+
+struct TuneKey {
+  int ptype, conn8, size_class, count_class;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(ptype, conn8, size_class, count_class) < std::tie(o.ptype, o.conn8, o.size_class, o.count_class);
+  }
+};
+
+pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, double h, bool conn8, bool autotune,
+                            cudaStream_t s, pg_batch_plan **out_plan) {
+  auto plan = std::make_unique<pg_batch_plan>();
+  PG_CUDA_TRY(cudaGetDevice(&plan->device), "cudaGetDevice");
+  plan->ptype = ins[0].ptype;
+  plan->conn8 = conn8;
+  plan->h = h;
+  const size_t es = (size_t)elem_size(plan->ptype);
+  std::vector<RImg> base((size_t)n);
+  int64_t pixels = 0;
+  for (int i = 0; i < n; ++i) {
+    const Dims d = dims_of(ins[i]);
+    RImg &im = base[(size_t)i];
+    im = RImg{};
+    im.mask = ins[i].data;
+    im.out = outs[i].data;
+    im.H = d.nz * d.ny;
+    im.W = d.nx;
+    pixels += im.H * im.W;
+  }
+  plan_tables(*plan, base, 64, plan->t64);
+  plan_tables(*plan, base, 32, plan->t32);
+  const int max_tiles = std::max(plan->t64.ntiles, plan->t32.ntiles);
+  const size_t off_flags = 256;
+  const size_t flags_bytes = ((sizeof(unsigned) * 2 * (size_t)max_tiles + 255) / 256) * 256;
+  const size_t off_tab64 = off_flags + flags_bytes;
+  const size_t tab_bytes = ((sizeof(RImg) * (size_t)n + 255) / 256) * 256;
+  const size_t off_tab32 = off_tab64 + tab_bytes;
+  size_t off_rec = off_tab32 + tab_bytes;
+  size_t rec_bytes = 0;
+  for (auto &im : base) rec_bytes += (es * (size_t)(im.H * im.W) + 255) / 256 * 256;
+  PG_CUDA_TRY(cudaMalloc(&plan->scratch, off_rec + rec_bytes + 256), "batch plan allocation");
+  plan->clear_bytes = off_tab64;
+  // reconstruction buffers, then device copies of both tile tables
+  char *b = static_cast<char *>(plan->scratch);
+  size_t off = off_rec;
+  for (size_t i = 0; i < base.size(); ++i) {
+    plan->t64.imgs[i].rec = b + off;
+    plan->t32.imgs[i].rec = b + off;
+    off += (es * (size_t)(base[i].H * base[i].W) + 255) / 256 * 256;
+  }
+  plan->t64.d_imgs = reinterpret_cast<RImg *>(b + off_tab64);
+  plan->t32.d_imgs = reinterpret_cast<RImg *>(b + off_tab32);
+  cudaError_t e = cudaMemcpy(plan->t64.d_imgs, plan->t64.imgs.data(), sizeof(RImg) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(plan->t32.d_imgs, plan->t32.imgs.data(), sizeof(RImg) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(plan->scratch);
+    return cuda_status(e, "upload batch tile tables");
+  }
+
+  static std::mutex mu;
+  static std::map<TuneKey, PlanCfg> cache;
+  const TuneKey key{plan->ptype, conn8 ? 1 : 0, (int)std::log2((double)std::max<int64_t>(pixels, 1)),
+                    (int)std::log2((double)std::max(n, 1))};
+  bool cached = false;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) { plan->cfg = it->second; cached = true; }
+  }
+  if (autotune && !cached) {
+    std::vector<PlanCfg> cands;
+    for (int rt : {64, 32}) {
+      if (es == 8 && rt == 64) continue;
+      for (int sw : {4, 16, kMaxSweeps}) cands.push_back(PlanCfg{rt, sw});
+    }
+    cudaEvent_t a, z;
+    PG_CUDA_TRY(cudaEventCreate(&a), "event");
+    PG_CUDA_TRY(cudaEventCreate(&z), "event");
+    float best = 1e30f;
+    for (const PlanCfg &c : cands) {
+      pg_status st = plan_run(*plan, c, s, nullptr);  // warm
+      if (st != PG_OK) { cudaEventDestroy(a); cudaEventDestroy(z); cudaFree(plan->scratch); return st; }
+      float tot = 0.f;
+      for (int r = 0; r < 2; ++r) {
+        cudaEventRecord(a, s);
+        plan_run(*plan, c, s, nullptr);
+        cudaEventRecord(z, s);
+        cudaEventSynchronize(z);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, z);
+        tot += ms;
+      }
+      if (tot < best) { best = tot; plan->cfg = c; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(z);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = plan->cfg;
+  } else if (!cached) {
+    plan->cfg = PlanCfg{es == 8 ? 32 : 64, kMaxSweeps};
+  }
+  *out_plan = plan.release();
+  return PG_OK;
+}
+
+pg_status run_batch_plan(pg_batch_plan *p, cudaStream_t s) {
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev != p->device) return fail(PG_ERR_INVALID_ARGUMENT, "batch plan used on another device");
+  return plan_run(*p, p->cfg, s, &p->grid);
+}
+
+void destroy_batch_plan(pg_batch_plan *p) {
+  if (!p) return;
+  if (p->scratch) cudaFree(p->scratch);
+  delete p;
 }
 
 // ------------------------------------------------------------------ allocation-free variant
@@ -681,6 +904,14 @@ pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const 
   else return pg::fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
   return pg::reconstruction_noalloc(type == PG_RECONSTRUCT_DILATE, conn8, *marker, *mask, *out,
                                     reinterpret_cast<cudaStream_t>(stream));
+}
+
+pg_status pg_batch_plan_config(const pg_batch_plan *plan, int32_t *tile, int32_t *sweeps, int32_t *grid) {
+  if (!plan) return pg::fail(PG_ERR_INVALID_ARGUMENT, "null plan");
+  if (tile) *tile = plan->cfg.rt;
+  if (sweeps) *sweeps = plan->cfg.sweeps;
+  if (grid) *grid = plan->grid;
+  return PG_OK;
 }
 
 }  // extern "C"

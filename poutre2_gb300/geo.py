@@ -108,3 +108,45 @@ def leveling(i_ref, i_marker, nl_static, o_img, check=None):
 
 def last_reconstruction_rounds() -> int:
     return int(_lib.load().pg_last_reconstruction_rounds())
+
+
+class HMaximaBinaryBatch:
+    """Prepared ragged batch of the binary h-maxima (``pg_h_maxima_binary_batch_plan``).
+
+    ``run()`` is one memset and one persistent launch over all images and can be captured in a
+    CUDA graph.  With ``autotune`` the tile side and the sweep sets per tile visit are chosen by
+    timing them on this batch (cached per pixel type, connectivity and size class).  The input
+    and output tensors must stay alive and in place while the plan is used."""
+
+    def __init__(self, imgs: Sequence[torch.Tensor], pvalue, nl_static, outs: Sequence[torch.Tensor],
+                 autotune: bool = True):
+        n = len(imgs)
+        if len(outs) != n or n == 0:
+            raise _lib.PoutreError(1, "HMaximaBinaryBatch: as many outputs as inputs (>= 1) are needed")
+        self._keep = (list(imgs), list(outs))
+        ins = (_lib.PgImage * n)(*[descriptor(t, "input") for t in imgs])
+        ous = (_lib.PgImage * n)(*[descriptor(t, "output") for t in outs])
+        self._plan = ctypes.c_void_p()
+        _lib.call("pg_h_maxima_binary_batch_plan", ins, ous, n, float(pvalue), int(Common_NL_SE(nl_static)),
+                  int(bool(autotune)), ctypes.byref(self._plan), _stream())
+
+    def run(self, check=False):
+        _lib.call("pg_batch_plan_run", self._plan, _stream())
+        _post(check)
+
+    @property
+    def config(self):
+        t, s, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _lib.call("pg_batch_plan_config", self._plan, ctypes.byref(t), ctypes.byref(s), ctypes.byref(g))
+        return {"tile": t.value, "sweeps_per_visit": s.value, "grid": g.value}
+
+    def close(self):
+        if self._plan:
+            _lib.load().pg_batch_plan_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

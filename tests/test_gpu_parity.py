@@ -311,6 +311,39 @@ def test_h_maxima_binary_and_batch():
         np.testing.assert_array_equal(host(single), host(o))
 
 
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int64])
+def test_batch_plan_autotuned_and_graph_replay(dt):
+    from poutre2_gb300 import geo, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    imgs = [synthetic.smoothed_noise_u8(hw, 300 + i).astype(dt) for i, hw in
+            enumerate([(64, 64), (130, 70), (1, 9), (200, 333), (65, 64), (97, 1)])]
+    xs = [dev(f) for f in imgs]
+    outs = [torch.empty(x.shape, dtype=torch.uint8, device="cuda") for x in xs]
+    plan = geo.HMaximaBinaryBatch(xs, 7, Common_NL_SE.SECross2D, outs, autotune=True)
+    assert plan.config["tile"] in (32, 64)
+    plan.run(check=True)
+    for f, o in zip(imgs, outs):
+        np.testing.assert_array_equal(host(o), oracle.h_maxima_binary(f, 7, "SECross2D"))
+    # the run captured in a CUDA graph and replayed reproduces the result
+    for o in outs:
+        o.zero_()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.run()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run()
+    for o in outs:
+        o.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    for f, o in zip(imgs, outs):
+        np.testing.assert_array_equal(host(o), oracle.h_maxima_binary(f, 7, "SECross2D"))
+    plan.close()
+
+
 @pytest.mark.parametrize("dt", TYPES)
 @pytest.mark.parametrize("kind", ["low_leveling", "high_leveling", "leveling"])
 def test_leveling(dt, kind):
