@@ -1,0 +1,134 @@
+// facade_test.cpp -- the reference's known-answer tests replayed through the C++ facade
+// (include/poutre_gb300/poutre.hpp), in the style of poutre2's Catch2 tests: parse images
+// with ImageFromString, call the poutre-named entry point, compare ImageToString.
+//
+// Usage: facade_test <cases file>; one case per line, fields separated by ';':
+//   op;se;param;input1;input2;expected     (input2 empty for one-input operators)
+// Exit status: number of failed cases (0 = all pass).
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "poutre_gb300/poutre.hpp"
+
+using namespace poutre::gb300;
+
+static std::vector<std::string> split(const std::string &s, char c) {
+  std::vector<std::string> out;
+  std::string cur;
+  std::istringstream is(s);
+  while (std::getline(is, cur, c)) out.push_back(cur);
+  if (!s.empty() && s.back() == c) out.push_back("");
+  return out;
+}
+
+static se::Common_NL_SE se_of(const std::string &n) {
+  static const std::map<std::string, se::Common_NL_SE> m = {
+      {"SESegmentX1D", se::Common_NL_SE::SESegmentX1D}, {"SESquare2D", se::Common_NL_SE::SESquare2D},
+      {"SECross2D", se::Common_NL_SE::SECross2D},       {"SESegmentX2D", se::Common_NL_SE::SESegmentX2D},
+      {"SESegmentY2D", se::Common_NL_SE::SESegmentY2D}, {"SESegmentX3D", se::Common_NL_SE::SESegmentX3D},
+      {"SESegmentY3D", se::Common_NL_SE::SESegmentY3D}, {"SESegmentZ3D", se::Common_NL_SE::SESegmentZ3D},
+      {"SECross3D", se::Common_NL_SE::SECross3D},       {"SESquare3D", se::Common_NL_SE::SESquare3D}};
+  return m.at(n);
+}
+
+// predefined runtime neighbour lists (src/structuring_element/predefined_nl_se.cpp:19-92)
+static se::NeighborList nl_of(const std::string &n) {
+  se::NeighborList nl;
+  if (n == "SESegmentX1D") { nl.rank = 1; nl.offsets = {0, -1, 1}; }
+  else if (n == "SESegmentX2D") nl.offsets = {0, 0, 0, -1, 0, 1};
+  else if (n == "SESegmentY2D") nl.offsets = {0, 0, -1, 0, 1, 0};
+  else if (n == "SESquare2D") nl.offsets = {0, 0, -1, -1, 0, -1, 1, -1, -1, 0, 1, 0, -1, 1, 0, 1, 1, 1};
+  else if (n == "SECross2D") nl.offsets = {0, 0, 0, -1, -1, 0, 1, 0, 0, 1};
+  else {
+    nl.rank = 3;
+    if (n == "SESegmentX3D") nl.offsets = {0, 0, 0, 0, 0, -1, 0, 0, 1};
+    else if (n == "SESegmentY3D") nl.offsets = {0, 0, 0, 0, -1, 0, 0, 1, 0};
+    else if (n == "SESegmentZ3D") nl.offsets = {0, 0, 0, -1, 0, 0, 1, 0, 0};
+    else if (n == "SECross3D") nl.offsets = {0, 0, 0, 0, 0, -1, 0, -1, 0, -1, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+    else {  // SESquare3D
+      nl.offsets = {0, 0, 0};
+      for (int c = -1; c <= 1; ++c)
+        for (int b = -1; b <= 1; ++b)
+          for (int a = -1; a <= 1; ++a)
+            if (a || b || c) nl.offsets.insert(nl.offsets.end(), {a, b, c});
+    }
+  }
+  return nl;
+}
+
+int main(int argc, char **argv) {
+  if (argc < 2) {
+    std::cerr << "usage: facade_test <cases>\n";
+    return 100;
+  }
+  std::ifstream f(argv[1]);
+  std::string line;
+  int failed = 0, run = 0;
+  while (std::getline(f, line)) {
+    if (line.empty()) continue;
+    auto v = split(line, ';');
+    if (v.size() != 6) { std::cerr << "bad case line\n"; return 101; }
+    const std::string &op = v[0], &sen = v[1];
+    const double param = v[2].empty() ? 0.0 : std::stod(v[2]);
+    try {
+      DeviceImage a = ImageFromString(v[3]);
+      DeviceImage o = CloneGeometry(a);
+      if (op == "dilate_static") Dilate(a, se_of(sen), 1, o);
+      else if (op == "erode_static") Erode(a, se_of(sen), 1, o);
+      else if (op == "dilate_nl") Dilate(a, nl_of(sen), o);
+      else if (op == "erode_nl") Erode(a, nl_of(sen), o);
+      else if (op == "dilatex") DilateX(a, (std::ptrdiff_t)param, o);
+      else if (op == "erodex") ErodeX(a, (std::ptrdiff_t)param, o);
+      else if (op == "dilatey") DilateY(a, (std::ptrdiff_t)param, o);
+      else if (op == "erodey") ErodeY(a, (std::ptrdiff_t)param, o);
+      else if (op == "reconstruct_dilate" || op == "reconstruct_erode") {
+        DeviceImage b = ImageFromString(v[4]);
+        geo::Reconstruction(op == "reconstruct_dilate" ? geo::reconstruction_type::dilate : geo::reconstruction_type::erode,
+                            a, b, se_of(sen), o);
+      } else if (op == "low_leveling" || op == "high_leveling" || op == "leveling") {
+        DeviceImage b = ImageFromString(v[4]);
+        if (op == "low_leveling") geo::low_leveling(a, b, se_of(sen), o);
+        else if (op == "high_leveling") geo::high_leveling(a, b, se_of(sen), o);
+        else geo::leveling(a, b, se_of(sen), o);
+      } else if (op == "h_minima") geo::h_minima(a, param, se_of(sen), o);
+      else if (op == "h_maxima") geo::h_maxima(a, param, se_of(sen), o);
+      else if (op == "h_concave") geo::h_concave(a, param, se_of(sen), o);
+      else if (op == "h_convex") geo::h_convex(a, param, se_of(sen), o);
+      else if (op == "dynamic_pseudo_opening") geo::dynamic_pseudo_opening(a, param, se_of(sen), o);
+      else if (op == "dynamic_pseudo_closing") geo::dynamic_pseudo_closing(a, param, se_of(sen), o);
+      else { std::cerr << "unknown op " << op << "\n"; return 102; }
+      ++run;
+      const std::string got = ImageToString(o);
+      if (got != v[5]) {
+        ++failed;
+        std::cerr << "FAIL " << op << " " << sen << "\n  got      " << got << "\n  expected " << v[5] << "\n";
+      }
+    } catch (const std::exception &e) {
+      ++failed;
+      std::cerr << "EXCEPTION " << op << " " << sen << ": " << e.what() << "\n";
+    }
+  }
+  // error behaviour: the reference throws std::runtime_error for these
+  int expected_throws = 0;
+  try {
+    DeviceImage a = ImageFromString("Scalar GUINT8 2 2 3 1 2 3 4 5 6");
+    Dilate(a, se::Common_NL_SE::SESquare2D, 1, a);  // output aliases the input
+  } catch (const std::runtime_error &) { ++expected_throws; }
+  try {
+    DeviceImage a = ImageFromString("Scalar GUINT8 2 2 3 1 2 3 4 5 6");
+    DeviceImage o = CloneGeometry(a);
+    DilateY(a, 1, o);  // non-square image
+  } catch (const std::runtime_error &) { ++expected_throws; }
+  try {
+    DeviceImage a = ImageFromString("Scalar GUINT8 2 2 3 1 2 3 4 5 6");
+    DeviceImage o = CloneGeometry(a);
+    Dilate(a, se::Common_NL_SE::SESquare3D, 1, o);  // SE rank differs from the image's
+  } catch (const std::runtime_error &) { ++expected_throws; }
+  if (expected_throws != 3) { std::cerr << "error behaviour differs\n"; ++failed; }
+  std::cout << "facade_test: " << run << " cases, " << failed << " failed\n";
+  return failed;
+}
