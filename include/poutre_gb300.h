@@ -176,16 +176,20 @@ PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *o
 /* A prepared ragged batch of the binary h-maxima (no reference counterpart): the image and tile
  * tables, the worklist and the reconstruction buffers stay on the device, so a run is one
  * memset plus one persistent cooperative launch, both of which can be captured in a CUDA graph.
- * With autotune != 0 the plan times tile side (64 or 32 pixels = threads per tile) x sweep sets
- * per tile visit (4, 16, unbounded) on this batch and keeps the fastest; the choice is cached per
- * (pixel type, connectivity, batch size class).  Inputs/outputs must stay valid while the plan
- * is used.  Plan creation synchronises the device. */
+ * With autotune != 0 the plan times tile side (32: register tiles, a warp per tile; 64: shared-
+ * memory tiles, a 64-thread CTA per tile) x sweep sets per tile visit (4, 16, unbounded) on this
+ * batch and keeps the fastest; the choice is cached per (pixel type, connectivity, batch size
+ * class).  Without autotune the configuration is 32 / unbounded.  Inputs/outputs must stay valid
+ * while the plan is used.  Plan creation synchronises the device.
+ * pg_batch_plan_set_config pins the configuration: tile 32 or 64 (64 only for pixels of at most
+ * 4 bytes), sweeps >= 1 (a tile that reaches the cap yields and is revisited next round). */
 typedef struct pg_batch_plan pg_batch_plan;
 PG_API pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, double h,
                                                int32_t common_se, int32_t autotune, pg_batch_plan **plan,
                                                pg_stream_t stream);
 PG_API pg_status pg_batch_plan_run(pg_batch_plan *plan, pg_stream_t stream);
 PG_API pg_status pg_batch_plan_config(const pg_batch_plan *plan, int32_t *tile, int32_t *sweeps, int32_t *grid);
+PG_API pg_status pg_batch_plan_set_config(pg_batch_plan *plan, int32_t tile, int32_t sweeps);
 PG_API pg_status pg_batch_plan_destroy(pg_batch_plan *plan);
 
 /* poutre::geo::low_leveling / high_leveling / leveling(const IInterface& ref, const IInterface& marker,

@@ -31,7 +31,8 @@ EXPORTED = [
     "pg_sat_sub_constant", "pg_sat_add_constant",
     "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
     "pg_check_device", "pg_last_reconstruction_rounds", "pg_reconstruction_noalloc",
-    "pg_h_maxima_binary_batch_plan", "pg_batch_plan_run", "pg_batch_plan_config", "pg_batch_plan_destroy",
+    "pg_h_maxima_binary_batch_plan", "pg_batch_plan_run", "pg_batch_plan_config", "pg_batch_plan_set_config",
+    "pg_batch_plan_destroy",
 ]
 
 
@@ -97,6 +98,7 @@ def load(path: str | None = None):
             "pg_h_maxima_binary_batch_plan": [img, img, I32, D, I32, I32, ctypes.POINTER(VP), VP],
             "pg_batch_plan_run": [VP, VP],
             "pg_batch_plan_config": [VP, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)],
+            "pg_batch_plan_set_config": [VP, I32, I32],
             "pg_batch_plan_destroy": [VP],
         }
         for name, args in sig.items():

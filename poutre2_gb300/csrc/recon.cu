@@ -105,8 +105,10 @@ __device__ __forceinline__ void set_status(RCtl *ctl, int code) {
   atomicCAS(&g_recon_status, 0, code);
 }
 
-// Grid barrier with a bounded wait.  Returns false once any CTA recorded an error.
+// Grid barrier with a bounded wait.  Returns false once any CTA recorded an error; thread 0
+// reads the status for its whole CTA so that every thread takes the same branch afterwards.
 __device__ bool grid_barrier(RCtl *ctl) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *genp = &ctl->bar_gen;
@@ -130,9 +132,10 @@ __device__ bool grid_barrier(RCtl *ctl) {
       }
     }
     __threadfence();
+    s_ok = *((volatile int *)&ctl->status) == 0;
   }
   __syncthreads();
-  return *((volatile int *)&ctl->status) == 0;
+  return s_ok != 0;
 }
 
 template <typename T, bool SUP>
@@ -140,7 +143,7 @@ __device__ __forceinline__ T sat_shift(T m, T h) {
   // marker of h-maxima (sat_sub) / h-minima (sat_add), op_Saturated_{Sub,Add}_Constant
   // (pixel_processing/details/arith_op_t.hpp:218-345), clamped to the pixel type's range
   if constexpr (std::is_integral_v<T>) {
-    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
+    using Wide = std::conditional_t<(sizeof(T) < 4), int, std::conditional_t<(sizeof(T) < 8), long long, __int128>>;
     const Wide r = SUP ? (Wide)m - (Wide)h : (Wide)m + (Wide)h;
     if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
     if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
@@ -150,27 +153,29 @@ __device__ __forceinline__ T sat_shift(T m, T h) {
   }
 }
 
-// effective mask and initial value of pixel i
+// Effective mask and initial value of a pixel from its loaded inputs -- `a` the mask (the
+// leveling reference), `mk` the marker, loaded only when needs_marker() says so -- kept apart
+// from the loads so that a caller can issue the loads of many pixels before it waits for the
+// first.  Round 0 starts from select_marker: min(marker, mask) (max for erosion).
+template <typename T>
+__device__ __forceinline__ bool needs_marker(const RParams<T> &P, int round) {
+  return P.init != INIT_SAT_CONST && (round == 0 || P.mask_mode != MASK_PLAIN);
+}
 template <typename T, bool SUP>
-__device__ __forceinline__ void pixel_init(const RImg &im, const RParams<T> &P, int64_t i, T &mask, T &init) {
-  const T a = ldg(static_cast<const T *>(im.mask) + i);
+__device__ __forceinline__ void combine_init(const RParams<T> &P, T a, T mk, T &mask, T &init) {
   if (P.init == INIT_SAT_CONST) {
     mask = a;
     init = sat_shift<T, SUP>(a, P.h);
     return;
   }
-  const T mk = ldg(static_cast<const T *>(im.marker) + i);
   if (P.mask_mode == MASK_MAX_MARKER) mask = Op<T, true>::apply(mk, a);
   else if (P.mask_mode == MASK_MIN_MARKER) mask = Op<T, false>::apply(mk, a);
   else mask = a;
-  init = Op<T, !SUP>::apply(mk, mask);  // select_marker: min(marker, mask) / max for erosion
+  init = Op<T, !SUP>::apply(mk, mask);
 }
-
-template <typename T, bool SUP>
-__device__ __forceinline__ T pixel_mask(const RImg &im, const RParams<T> &P, int64_t i) {
-  const T a = ldg(static_cast<const T *>(im.mask) + i);
+template <typename T>
+__device__ __forceinline__ T combine_mask(const RParams<T> &P, T a, T mk) {
   if (P.init == INIT_SAT_CONST || P.mask_mode == MASK_PLAIN) return a;
-  const T mk = ldg(static_cast<const T *>(im.marker) + i);
   return P.mask_mode == MASK_MAX_MARKER ? Op<T, true>::apply(mk, a) : Op<T, false>::apply(mk, a);
 }
 
@@ -189,6 +194,37 @@ template <typename T> __device__ __forceinline__ void st_cg(T *p, T v) {
 
 enum : int { B_N = 1, B_S = 2, B_W = 4, B_E = 8, B_NW = 16, B_NE = 32, B_SW = 64, B_SE = 128, B_SELF = 256 };
 
+// Puts the tiles next to tile (tx, ty) whose shared border changed (f: B_* bits) on the next
+// round's worklist, and the tile itself when it yielded before its local fixpoint.
+template <bool CONN8>
+__device__ void flag_neighbours(const RImg &im, unsigned *flags, int ntiles, RCtl *ctl, int round, int tx, int ty,
+                                int f) {
+  unsigned *fnext = flags + (size_t)((round + 1) & 1) * ntiles;
+  auto flag = [&](int dx, int dy) {
+    const int nx = tx + dx, ny = ty + dy;
+    if (nx < 0 || ny < 0 || nx >= im.tiles_x || ny >= im.tiles_y) return;
+    fnext[im.tile_begin + ny * im.tiles_x + nx] = 1u;
+  };
+  if (f & B_N) flag(0, -1);
+  if (f & B_S) flag(0, 1);
+  if (f & B_W) flag(-1, 0);
+  if (f & B_E) flag(1, 0);
+  if (CONN8) {
+    if (f & B_NW) flag(-1, -1);
+    if (f & B_NE) flag(1, -1);
+    if (f & B_SW) flag(-1, 1);
+    if (f & B_SE) flag(1, 1);
+  }
+  if (f & B_SELF) flag(0, 0);
+  // a changed corner pixel is also on a changed edge, so the edge bits cover every flag.  The
+  // word is read before it is written: thousands of tiles set it in a busy round, and the
+  // same-address writes would queue at one L2 slice.
+  if (f & (B_N | B_S | B_W | B_E | B_SELF)) {
+    volatile unsigned *any = &ctl->any[(round + 1) % 3];
+    if (*any == 0u) *any = 1u;
+  }
+}
+
 template <typename T, bool SUP, bool CONN8, int RT>
 __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, int round, T *s_out, T *s_mask,
                              int *s_flag) {
@@ -200,23 +236,47 @@ __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, i
   const int64_t y0 = (int64_t)ty * RT, x0 = (int64_t)tx * RT;
   const T *rec_in = static_cast<const T *>(im.rec);
 
-  // stage: current reconstruction (round 0: marker) with halo, effective mask
-  for (int i = threadIdx.x; i < (RT + 2) * (RT + 2); i += RTHREADS) {
-    const int r = i / (RT + 2) - 1, c = i % (RT + 2) - 1;
-    const int64_t gy = y0 + r, gx = x0 + c;
-    const bool inside = gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
-    const bool interior = r >= 0 && r < RT && c >= 0 && c < RT;
-    T v = NEU, m = NEU;
-    if (inside) {
-      const int64_t gi = gy * im.W + gx;
-      if (round == 0) pixel_init<T, SUP>(im, P, gi, m, v);
-      else {
-        v = ld_cg(rec_in + gi);
-        if (interior) m = pixel_mask<T, SUP>(im, P, gi);
-      }
+  // stage: current reconstruction (round 0: marker) with halo, effective mask.  Eight pixels
+  // per thread at a time: their loads (at clamped, always valid addresses) are all issued
+  // before the first shared-memory store.
+  constexpr int NEL = (RT + 2) * (RT + 2);
+  constexpr int ITER = (NEL + RTHREADS - 1) / RTHREADS;
+  constexpr int CH = 8;
+  const bool need_mk = needs_marker(P, round);
+  const T *ms_in = static_cast<const T *>(im.mask);
+  const T *mk_in = static_cast<const T *>(im.marker);
+  for (int k0 = 0; k0 < ITER; k0 += CH) {
+    T a[CH], b[CH], c[CH];
+#pragma unroll
+    for (int k = 0; k < CH; ++k) {
+      const int i = (k0 + k) * RTHREADS + threadIdx.x;
+      const int r = i / (RT + 2) - 1, cc = i % (RT + 2) - 1;
+      const int64_t gy = y0 + r, gx = x0 + cc;
+      const bool inside = i < NEL && gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
+      const int64_t gi = inside ? gy * im.W + gx : 0;
+      a[k] = ldg(ms_in + gi);
+      b[k] = need_mk ? ldg(mk_in + gi) : a[k];
+      c[k] = round > 0 ? ld_cg(rec_in + gi) : a[k];
     }
-    s_out[(r + 1) * PO + (c + 1)] = v;
-    if (interior) s_mask[r * PM + c] = m;
+#pragma unroll
+    for (int k = 0; k < CH; ++k) {
+      const int i = (k0 + k) * RTHREADS + threadIdx.x;
+      if (i >= NEL) break;
+      const int r = i / (RT + 2) - 1, cc = i % (RT + 2) - 1;
+      const int64_t gy = y0 + r, gx = x0 + cc;
+      const bool inside = gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
+      const bool interior = r >= 0 && r < RT && cc >= 0 && cc < RT;
+      T v = NEU, m = NEU;
+      if (inside) {
+        if (round == 0) combine_init<T, SUP>(P, a[k], b[k], m, v);
+        else {
+          v = c[k];
+          m = combine_mask(P, a[k], b[k]);
+        }
+      }
+      s_out[(r + 1) * PO + (cc + 1)] = v;
+      if (interior) s_mask[r * PM + cc] = m;
+    }
   }
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
@@ -243,6 +303,7 @@ __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, i
     return false;
   };
   const int lane = threadIdx.x;  // column for vertical sweeps, row for horizontal ones
+  bool changed = false;          // any pixel of the tile changed during this visit
   for (int sweep = 0; sweep < P.max_sweeps; ++sweep) {
     bool ch = false;
     // down: neighbours in the row above
@@ -284,41 +345,25 @@ __device__ void process_tile(const RImg &im, const RParams<T> &P, int t_local, i
       converged = true;
       break;
     }
+    changed = true;
   }
   if (!converged) bflags |= B_SELF;
   if (bflags) atomicOr(s_flag, bflags);
   __syncthreads();
   const int f = *s_flag;
 
-  // write back (round 0 always: the marker itself is new) and flag the neighbours
+  // write back (round 0 always: the marker itself is new; later rounds whenever a pixel
+  // changed -- an interior-only change happens when the previous visit yielded) and flag the
+  // neighbours
   T *rec = static_cast<T *>(im.rec);
-  if (round == 0 || f != 0) {
+  if (round == 0 || changed) {
     for (int i = threadIdx.x; i < RT * RT; i += RTHREADS) {
       const int r = i / RT, c = i % RT;
       const int64_t gy = y0 + r, gx = x0 + c;
       if (gy < im.H && gx < im.W) st_cg(rec + gy * im.W + gx, s_out[(r + 1) * PO + (c + 1)]);
     }
   }
-  if (threadIdx.x == 0 && f != 0) {
-    unsigned *fnext = P.flags + (size_t)((round + 1) & 1) * P.ntiles;
-    auto flag = [&](int dx, int dy) {
-      const int nx = tx + dx, ny = ty + dy;
-      if (nx < 0 || ny < 0 || nx >= im.tiles_x || ny >= im.tiles_y) return;
-      fnext[im.tile_begin + ny * im.tiles_x + nx] = 1u;
-    };
-    if (f & B_N) flag(0, -1);
-    if (f & B_S) flag(0, 1);
-    if (f & B_W) flag(-1, 0);
-    if (f & B_E) flag(1, 0);
-    if (CONN8) {
-      if (f & B_NW) flag(-1, -1);
-      if (f & B_NE) flag(1, -1);
-      if (f & B_SW) flag(-1, 1);
-      if (f & B_SE) flag(1, 1);
-    }
-    if (f & B_SELF) flag(0, 0);
-    if (f & (B_N | B_S | B_W | B_E | B_SELF)) atomicExch(&P.ctl->any[(round + 1) % 3], 1u);
-  }
+  if (threadIdx.x == 0 && f != 0) flag_neighbours<CONN8>(im, P.flags, P.ntiles, P.ctl, round, tx, ty, f);
   __syncthreads();
 }
 
@@ -332,6 +377,28 @@ __device__ __forceinline__ const RImg &image_of(const RParams<T> &P, int tile, i
   }
   t_local = tile - P.imgs[lo].tile_begin;
   return P.imgs[lo];
+}
+
+// Epilogue over every pixel of every image, after the last round: the binary h-maxima
+// comparison or the leveling clip by the reference.
+template <typename T, bool SUP>
+__device__ void recon_epilogue(const RParams<T> &P) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int k = 0; k < P.nimg; ++k) {
+    const RImg &im = (P.nimg == 1) ? P.single : P.imgs[k];
+    const int64_t n = im.H * im.W;
+    const T *rec = static_cast<const T *>(im.rec);
+    const T *ref = static_cast<const T *>(im.mask);
+    if (P.epi == EPI_BINARY_SUP) {
+      uint8_t *o = static_cast<uint8_t *>(im.out);
+      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        o[i] = (ldg(ref + i) > ld_cg(rec + i)) ? 255 : 0;
+    } else {  // EPI_CLIP_REF: low leveling min(rec, ref), high leveling max(rec, ref)
+      T *o = static_cast<T *>(im.out);
+      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        o[i] = Op<T, !SUP>::apply(ld_cg(rec + i), ldg(ref + i));
+    }
+  }
 }
 
 template <typename T, bool SUP, bool CONN8, int RT = tile_side<T>()>
@@ -383,30 +450,316 @@ __global__ void __launch_bounds__(RT) k_reconstruct(RParams<T> P) {
     g_recon_rounds = round;
   }
   if (!ok || P.epi == EPI_NONE) return;
+  recon_epilogue<T, SUP>(P);
+}
 
-  // epilogue over every pixel of every image
-  const int64_t stride = (int64_t)gridDim.x * RTHREADS;
-  for (int k = 0; k < P.nimg; ++k) {
-    const RImg &im = (P.nimg == 1) ? P.single : P.imgs[k];
-    const int64_t n = im.H * im.W;
-    const T *rec = static_cast<const T *>(im.rec);
-    const T *ref = static_cast<const T *>(im.mask);
-    if (P.epi == EPI_BINARY_SUP) {
-      uint8_t *o = static_cast<uint8_t *>(im.out);
-      for (int64_t i = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; i < n; i += stride)
-        o[i] = (ldg(ref + i) > ld_cg(rec + i)) ? 255 : 0;
-    } else {  // EPI_CLIP_REF: low leveling min(rec, ref), high leveling max(rec, ref)
-      T *o = static_cast<T *>(im.out);
-      for (int64_t i = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; i < n; i += stride)
-        o[i] = Op<T, !SUP>::apply(ld_cg(rec + i), ldg(ref + i));
+// ------------------------------------------------------------------ register tiles
+// For pixels of at most 4 bytes the tiles are 32x32 and one warp owns a tile with its values in
+// registers: for the vertical sweeps lane c holds column c (v[r] = row r), for the horizontal
+// ones the tile goes through shared memory once each way and lane r holds row r.
+//  * down / up sweeps take the three pixels of the previous row (8-connected; the same column
+//    4-connected), the neighbours' columns by warp shuffles;
+//  * right / left sweeps take only the pixel before in the row, a chain inside each lane's
+//    registers.  The diagonal relations inside the tile are all covered by the vertical sweeps,
+//    and every halo pixel's relations by the one-off halo values below, so a sweep set that
+//    changes nothing still means a local fixpoint of the full neighbourhood;
+//  * the mask is read from shared memory in either layout (pitch 33 words: conflict-free).
+// About one instruction per pixel and sweep set, against some seventy for the shared-memory
+// tile above; a CTA holds kRegWarps independent warps.
+static constexpr int kRegWarps = 4;
+static constexpr int kRP = 33;  // pitch in words of the per-warp shared arrays
+
+template <typename T> using RegS = std::conditional_t<(sizeof(T) < 4), uint32_t, T>;
+
+// Mask reads inside the sweeps: a volatile shared load is performed where it is written, so the
+// compiler does not keep the whole 32x32 mask in registers across sweeps (which would cost 64
+// registers per thread and most of the occupancy).
+template <typename T> __device__ __forceinline__ T lds_mask(const RegS<T> *p) {
+  const unsigned addr = (unsigned)__cvta_generic_to_shared(p);
+  uint32_t r;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(r) : "r"(addr));
+  if constexpr (std::is_same_v<T, float>) return __uint_as_float(r);
+  else return (T)r;
+}
+
+template <typename T> __device__ __forceinline__ T shfl_up1(T v) {
+  if constexpr (sizeof(T) < 4) return (T)__shfl_up_sync(0xffffffffu, (unsigned)v, 1);
+  else return __shfl_up_sync(0xffffffffu, v, 1);
+}
+template <typename T> __device__ __forceinline__ T shfl_dn1(T v) {
+  if constexpr (sizeof(T) < 4) return (T)__shfl_down_sync(0xffffffffu, (unsigned)v, 1);
+  else return __shfl_down_sync(0xffffffffu, v, 1);
+}
+
+// Pixel (gy, gx) seen from a neighbouring tile: neutral outside the image, the marker in round
+// 0, the current reconstruction later.  halo_load issues the loads (at a clamped, always valid
+// address), halo_finish combines them, so that all halo loads of a visit are in flight at once.
+template <typename T> struct HaloPx {
+  T a, mk;
+  bool in;
+};
+template <typename T>
+__device__ __forceinline__ HaloPx<T> halo_load(const RImg &im, const RParams<T> &P, int round, bool need_mk,
+                                               int64_t gy, int64_t gx) {
+  HaloPx<T> h;
+  h.in = gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
+  const int64_t gi = h.in ? gy * im.W + gx : 0;
+  if (round == 0) {
+    h.a = ldg(static_cast<const T *>(im.mask) + gi);
+    h.mk = need_mk ? ldg(static_cast<const T *>(im.marker) + gi) : h.a;
+  } else {
+    h.a = ld_cg(static_cast<const T *>(im.rec) + gi);
+    h.mk = h.a;
+  }
+  return h;
+}
+template <typename T, bool SUP>
+__device__ __forceinline__ T halo_finish(const RParams<T> &P, int round, const HaloPx<T> &h) {
+  if (!h.in) return Op<T, SUP>::neutral();
+  if (round > 0) return h.a;
+  T m, v;
+  combine_init<T, SUP>(P, h.a, h.mk, m, v);
+  return v;
+}
+
+template <typename T, bool SUP, bool CONN8>
+__device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_local, int round, RegS<T> *s_m,
+                                 RegS<T> *s_t) {
+  using OS = Op<T, SUP>;   // propagation
+  using OC = Op<T, !SUP>;  // clip by the mask
+  const int lane = threadIdx.x & 31;
+  const T NEU = OS::neutral();
+  const int tx = t_local % im.tiles_x, ty = t_local / im.tiles_x;
+  const int64_t y0 = (int64_t)ty * 32, x0 = (int64_t)tx * 32;
+  const T *rec_in = static_cast<const T *>(im.rec);
+  const int64_t gx = x0 + lane;
+  const bool colin = gx < im.W;
+
+  // stage, lane = column: tile values and mask (pixels outside the image: neutral, fixed).
+  // Loads come first, 16 rows at a time, so that they are all in flight together; the
+  // addresses of pixels outside the image are clamped to pixel 0 and the values discarded.
+  const T *mk_in = static_cast<const T *>(im.marker);
+  const T *ms_in = static_cast<const T *>(im.mask);
+  const bool need_mk = needs_marker(P, round);
+  T v[32];
+#pragma unroll
+  for (int h = 0; h < 32; h += 16) {
+    T a[16], b[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int64_t gy = y0 + h + r;
+      const int64_t gi = (colin && gy < im.H) ? gy * im.W + gx : 0;
+      a[r] = ldg(ms_in + gi);
+      b[r] = need_mk ? ldg(mk_in + gi) : a[r];
+      if (round > 0) v[h + r] = ld_cg(rec_in + gi);
+    }
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const bool ok = colin && y0 + h + r < im.H;
+      T m;
+      if (round == 0) combine_init<T, SUP>(P, a[r], b[r], m, v[h + r]);
+      else m = combine_mask(P, a[r], b[r]);
+      if (!ok) {
+        m = NEU;
+        v[h + r] = NEU;
+      }
+      s_m[(h + r) * kRP + lane] = m;
     }
   }
+  // Halo.  Its values stay fixed during the visit, so each halo pixel's contribution is
+  // folded into one value per border pixel: `top`/`bot` per column (lane = column: the three
+  // pixels above / below), `hl`/`hr` per row (lane = row: the three pixels left / right; one
+  // in 4-connectivity).  The sweeps apply them at the tile's first/last row and column.
+  T top, bot, hl, hr;
+  {
+    HaloPx<T> q[12];
+    q[0] = halo_load(im, P, round, need_mk, y0 - 1, gx);
+    q[1] = halo_load(im, P, round, need_mk, y0 + 32, gx);
+    q[2] = halo_load(im, P, round, need_mk, y0 + lane, x0 - 1);
+    q[3] = halo_load(im, P, round, need_mk, y0 + lane, x0 + 32);
+    if (CONN8) {
+      q[4] = halo_load(im, P, round, need_mk, y0 - 1, gx - 1);
+      q[5] = halo_load(im, P, round, need_mk, y0 - 1, gx + 1);
+      q[6] = halo_load(im, P, round, need_mk, y0 + 32, gx - 1);
+      q[7] = halo_load(im, P, round, need_mk, y0 + 32, gx + 1);
+      q[8] = halo_load(im, P, round, need_mk, y0 + lane - 1, x0 - 1);
+      q[9] = halo_load(im, P, round, need_mk, y0 + lane + 1, x0 - 1);
+      q[10] = halo_load(im, P, round, need_mk, y0 + lane - 1, x0 + 32);
+      q[11] = halo_load(im, P, round, need_mk, y0 + lane + 1, x0 + 32);
+    }
+    top = halo_finish<T, SUP>(P, round, q[0]);
+    bot = halo_finish<T, SUP>(P, round, q[1]);
+    hl = halo_finish<T, SUP>(P, round, q[2]);
+    hr = halo_finish<T, SUP>(P, round, q[3]);
+    if (CONN8) {
+      top = OS::apply(top, OS::apply(halo_finish<T, SUP>(P, round, q[4]), halo_finish<T, SUP>(P, round, q[5])));
+      bot = OS::apply(bot, OS::apply(halo_finish<T, SUP>(P, round, q[6]), halo_finish<T, SUP>(P, round, q[7])));
+      hl = OS::apply(hl, OS::apply(halo_finish<T, SUP>(P, round, q[8]), halo_finish<T, SUP>(P, round, q[9])));
+      hr = OS::apply(hr, OS::apply(halo_finish<T, SUP>(P, round, q[10]), halo_finish<T, SUP>(P, round, q[11])));
+    }
+  }
+  // staged borders, to tell afterwards which neighbours must be revisited
+#pragma unroll
+  for (int r = 0; r < 32; ++r) s_t[r * kRP + lane] = v[r];
+  __syncwarp();
+  const T initL = (T)s_t[lane * kRP], initR = (T)s_t[lane * kRP + 31];
+  const T initT = v[0], initB = v[31];
+  __syncwarp();
+
+  bool converged = false, changed = false, wch = false, ech = false;
+  for (int sweep = 0; sweep < P.max_sweeps; ++sweep) {
+    bool ch = false;
+    // down: the row above (lane 0 / 31 get their own value back from the shuffle: the pixels
+    // beyond the tile's side columns are halo, applied by the horizontal sweeps)
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      T nb;
+      if (r == 0) nb = top;
+      else {
+        nb = v[r - 1];
+        if (CONN8) nb = OS::apply(nb, OS::apply(shfl_up1(nb), shfl_dn1(nb)));
+      }
+      const T nv = OC::apply(OS::apply(v[r], nb), lds_mask<T>(s_m + r * kRP + lane));
+      ch |= nv != v[r];
+      v[r] = nv;
+    }
+    // up: the row below
+#pragma unroll
+    for (int r = 31; r >= 0; --r) {
+      T nb;
+      if (r == 31) nb = bot;
+      else {
+        nb = v[r + 1];
+        if (CONN8) nb = OS::apply(nb, OS::apply(shfl_up1(nb), shfl_dn1(nb)));
+      }
+      const T nv = OC::apply(OS::apply(v[r], nb), lds_mask<T>(s_m + r * kRP + lane));
+      ch |= nv != v[r];
+      v[r] = nv;
+    }
+    // to lane = row
+#pragma unroll
+    for (int r = 0; r < 32; ++r) s_t[r * kRP + lane] = v[r];
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = (T)s_t[lane * kRP + c];
+    __syncwarp();
+    // right: the pixel on the left; left: the pixel on the right
+    T prev = hl;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      const T nv = OC::apply(OS::apply(v[c], prev), lds_mask<T>(s_m + lane * kRP + c));
+      ch |= nv != v[c];
+      v[c] = nv;
+      prev = nv;
+    }
+    prev = hr;
+#pragma unroll
+    for (int c = 31; c >= 0; --c) {
+      const T nv = OC::apply(OS::apply(v[c], prev), lds_mask<T>(s_m + lane * kRP + c));
+      ch |= nv != v[c];
+      v[c] = nv;
+      prev = nv;
+    }
+    wch = v[0] != initL;
+    ech = v[31] != initR;
+    // back to lane = column
+#pragma unroll
+    for (int c = 0; c < 32; ++c) s_t[lane * kRP + c] = v[c];
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; ++r) v[r] = (T)s_t[r * kRP + lane];
+    __syncwarp();
+    if (!__any_sync(0xffffffffu, ch)) {
+      converged = true;
+      break;
+    }
+    changed = true;
+  }
+
+  const unsigned bN = __ballot_sync(0xffffffffu, v[0] != initT);
+  const unsigned bS = __ballot_sync(0xffffffffu, v[31] != initB);
+  const unsigned bW = __ballot_sync(0xffffffffu, wch);
+  const unsigned bE = __ballot_sync(0xffffffffu, ech);
+  int f = converged ? 0 : B_SELF;
+  if (bN) f |= B_N;
+  if (bS) f |= B_S;
+  if (bW) f |= B_W;
+  if (bE) f |= B_E;
+  if (bN & 1u) f |= B_NW;
+  if (bN >> 31) f |= B_NE;
+  if (bS & 1u) f |= B_SW;
+  if (bS >> 31) f |= B_SE;
+
+  if (round == 0 || changed) {
+    // the row stride goes through a shuffle so that the compiler recomputes these addresses
+    // here instead of keeping the stage's 32 row addresses alive across the sweeps
+    const long long Wd = __shfl_sync(0xffffffffu, (long long)im.W, 0);
+    T *p = static_cast<T *>(im.rec) + (y0 * Wd + gx);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      if (colin && y0 + r < im.H) st_cg(p, v[r]);
+      p += Wd;
+    }
+  }
+  if (lane == 0 && f != 0) flag_neighbours<CONN8>(im, P.flags, P.ntiles, P.ctl, round, tx, ty, f);
+  __syncwarp();
+}
+
+template <typename T, bool SUP, bool CONN8>
+__global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_reg(RParams<T> P) {
+  static_assert(sizeof(T) <= 4, "register tiles hold pixels of at most 4 bytes");
+  __shared__ RegS<T> s_m[kRegWarps][32 * kRP];
+  __shared__ RegS<T> s_t[kRegWarps][32 * kRP];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  RCtl *ctl = P.ctl;
+  const int wstride = gridDim.x * kRegWarps;
+
+  int round = 0;
+  bool ok = true;
+  for (;;) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->any[(round + 2) % 3] = 0u;
+    unsigned *fcur = P.flags + (size_t)(round & 1) * P.ntiles;
+    for (int t = blockIdx.x * kRegWarps + warp; t < P.ntiles; t += wstride) {
+      int a = 1;
+      if (round > 0) {
+        if (lane == 0) {
+          a = *((volatile unsigned *)(fcur + t)) != 0u;
+          if (a) fcur[t] = 0u;
+        }
+        a = __shfl_sync(0xffffffffu, a, 0);
+      }
+      if (a) {
+        int tl = 0;
+        const RImg &im = image_of(P, t, tl);
+        process_tile_reg<T, SUP, CONN8>(im, P, tl, round, s_m[warp], s_t[warp]);
+      }
+    }
+    if (!grid_barrier(ctl)) { ok = false; break; }
+    const unsigned any = *((volatile unsigned *)&ctl->any[(round + 1) % 3]);
+    ++round;
+    if (!any) break;
+    if (round >= P.max_rounds) {
+      if (threadIdx.x == 0) set_status(ctl, PG_ERR_NOT_CONVERGED);
+      ok = false;
+      break;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->rounds = round;
+    g_recon_rounds = round;
+  }
+  if (!ok || P.epi == EPI_NONE) return;
+  recon_epilogue<T, SUP>(P);
 }
 
 // ------------------------------------------------------------------ host side
 template <typename T, bool SUP, bool CONN8>
 static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool binary, cudaStream_t s) {
-  constexpr int RT = tile_side<T>(), RTHREADS = RT;
+  // register tiles (32x32, a warp each) up to 4-byte pixels, shared-memory tiles for 8-byte ones
+  constexpr bool REG = sizeof(T) <= 4;
+  constexpr int RT = REG ? 32 : tile_side<T>();
+  constexpr int RTHREADS = REG ? kRegWarps * 32 : RT;
+  constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
   int ntiles = 0;
   size_t rec_bytes = 0;
   for (auto &im : imgs) {
@@ -457,7 +810,9 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   P.epi = rq.epi;
   P.h = static_cast<T>(rq.h);
 
-  auto kern = k_reconstruct<T, SUP, CONN8>;
+  void (*kern)(RParams<T>) = nullptr;
+  if constexpr (REG) kern = k_reconstruct_reg<T, SUP, CONN8>;
+  else kern = k_reconstruct<T, SUP, CONN8>;
   int dev = 0;
   PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
   static std::mutex mu;
@@ -473,7 +828,7 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   }
   if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
   int grid = per_sm * num_sms();
-  if (grid > ntiles) grid = ntiles;
+  if (grid > ceil_div(ntiles, TILES_PER_CTA)) grid = (int)ceil_div(ntiles, TILES_PER_CTA);
 
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)grid);
@@ -518,10 +873,10 @@ pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, 
 // ------------------------------------------------------------------ batch plans + autotuner
 // A plan keeps a ragged batch's image tables, worklist and reconstruction buffers on the device
 // so that each run is one memset and one cooperative launch (both capturable in a CUDA graph).
-// The autotuner times the candidate configurations -- tile side (64 or 32 pixels, i.e. 64 or
-// 32 threads per tile) x sweep sets per tile visit before the tile yields to the next global
-// round (4, 16, unbounded) -- on the plan's own batch and keeps the fastest; the choice is
-// cached per (pixel type, connectivity, batch size class).
+// The autotuner times the candidate configurations -- tile side (32: register tiles, 64: shared-
+// memory tiles) x sweep sets per tile visit before the tile yields to the next global round
+// (4, 16, unbounded) -- on the plan's own batch and keeps the fastest; the choice is cached per
+// (pixel type, connectivity, batch size class).
 struct PlanCfg {
   int rt = 64;
   int sweeps = kMaxSweeps;
@@ -567,17 +922,23 @@ static pg_status plan_launch_t(pg_batch_plan &p, int sweeps, cudaStream_t s, int
   P.mask_mode = MASK_PLAIN;
   P.epi = EPI_BINARY_SUP;
   P.h = static_cast<T>(p.h);
-  auto kern = k_reconstruct<T, true, CONN8, RT>;
+  // 32-pixel tiles of pixels up to 4 bytes run as register tiles (a warp per tile)
+  constexpr bool REG = RT == 32 && sizeof(T) <= 4;
+  constexpr int THREADS = REG ? kRegWarps * 32 : RT;
+  constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
+  void (*kern)(RParams<T>) = nullptr;
+  if constexpr (REG) kern = k_reconstruct_reg<T, true, CONN8>;
+  else kern = k_reconstruct<T, true, CONN8, RT>;
   int per_sm = 0;
-  PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RT, 0), "occupancy");
+  PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, 0), "occupancy");
   if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
   int grid = per_sm * num_sms();
-  if (grid > tb.ntiles) grid = tb.ntiles;
+  if (grid > ceil_div(tb.ntiles, TILES_PER_CTA)) grid = (int)ceil_div(tb.ntiles, TILES_PER_CTA);
   if (grid_out) *grid_out = grid;
   PG_CUDA_TRY(cudaMemsetAsync(p.scratch, 0, p.clear_bytes, s), "clear batch worklist");
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(RT);
+  cfg.blockDim = dim3(THREADS);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -714,7 +1075,7 @@ pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, do
     std::lock_guard<std::mutex> lk(mu);
     cache[key] = plan->cfg;
   } else if (!cached) {
-    plan->cfg = PlanCfg{es == 8 ? 32 : 64, kMaxSweeps};
+    plan->cfg = PlanCfg{32, kMaxSweeps};
   }
   *out_plan = plan.release();
   return PG_OK;
@@ -904,6 +1265,16 @@ pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const 
   else return pg::fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
   return pg::reconstruction_noalloc(type == PG_RECONSTRUCT_DILATE, conn8, *marker, *mask, *out,
                                     reinterpret_cast<cudaStream_t>(stream));
+}
+
+pg_status pg_batch_plan_set_config(pg_batch_plan *plan, int32_t tile, int32_t sweeps) {
+  if (!plan) return pg::fail(PG_ERR_INVALID_ARGUMENT, "null plan");
+  if (tile != 32 && tile != 64) return pg::fail(PG_ERR_INVALID_ARGUMENT, "batch plan tile side must be 32 or 64");
+  if (tile == 64 && pg::elem_size(plan->ptype) == 8)
+    return pg::fail(PG_ERR_INVALID_ARGUMENT, "batch plan tile side 64 needs pixels of at most 4 bytes");
+  if (sweeps < 1) return pg::fail(PG_ERR_INVALID_ARGUMENT, "batch plan sweeps per visit must be >= 1");
+  plan->cfg = pg::PlanCfg{tile, sweeps};
+  return PG_OK;
 }
 
 pg_status pg_batch_plan_config(const pg_batch_plan *plan, int32_t *tile, int32_t *sweeps, int32_t *grid) {

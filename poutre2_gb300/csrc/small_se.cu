@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "words.cuh"
 
 namespace pg {
 
@@ -32,6 +33,75 @@ template <typename T> struct Scalar {
   __device__ __forceinline__ Scalar shl(T left) const { Scalar r; r.e0 = left; return r; }
   __device__ __forceinline__ Scalar shr(T right) const { Scalar r; r.e0 = right; return r; }
 };
+
+// 16 u8 pixels held as eight words: for each 32-bit word of the pack its even bytes (bits 0-7,
+// 16-23) and its odd bytes (bits 8-15, 24-31) with the other bytes zeroed.  max/min of u8 pairs
+// is then the native 2x16-bit max/min (the odd bytes compare as x << 8), two instructions per
+// word, where a packed 4x8-bit max/min is emulated by a much longer sequence.
+struct PackU8S {
+  static constexpr int N = 16;
+  static constexpr uint32_t ME = 0x00ff00ffu, MO = 0xff00ff00u;
+  uint32_t e[4], o[4];
+  __device__ __forceinline__ void split(const uint32_t (&w)[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { e[i] = w[i] & ME; o[i] = w[i] & MO; }
+  }
+  __device__ __forceinline__ static PackU8S load(const uint8_t *p) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    PackU8S r;
+    r.split(w);
+    return r;
+  }
+  __device__ __forceinline__ void store(uint8_t *p) const {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(e[0] | o[0], e[1] | o[1], e[2] | o[2], e[3] | o[3]);
+  }
+  __device__ __forceinline__ static PackU8S fill(uint8_t x) {
+    const uint32_t s = (uint32_t)x * 0x01010101u;
+    PackU8S r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) { r.e[i] = s & ME; r.o[i] = s & MO; }
+    return r;
+  }
+  template <bool SUP> __device__ __forceinline__ static PackU8S op(const PackU8S &a, const PackU8S &b) {
+    PackU8S r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      r.e[i] = wop<uint16_t, SUP>(a.e[i], b.e[i]);
+      r.o[i] = wop<uint16_t, SUP>(a.o[i], b.o[i]);
+    }
+    return r;
+  }
+  __device__ __forceinline__ PackU8S shl(uint8_t left) const {
+    uint32_t w[4];
+    uint32_t prev = (uint32_t)left << 24;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t x = e[i] | o[i];
+      w[i] = __funnelshift_l(prev, x, 8);
+      prev = x;
+    }
+    PackU8S r;
+    r.split(w);
+    return r;
+  }
+  __device__ __forceinline__ PackU8S shr(uint8_t right) const {
+    uint32_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const uint32_t x = e[i] | o[i];
+      const uint32_t next = (i < 3) ? (e[i + 1] | o[i + 1]) : (uint32_t)right;
+      w[i] = __funnelshift_r(x, next, 8);
+    }
+    PackU8S r;
+    r.split(w);
+    return r;
+  }
+};
+
+// the pack type of a pixel type: split words for u8, plain 16-byte packs otherwise
+template <typename T> struct PackOf { using type = Pack<T>; };
+template <> struct PackOf<uint8_t> { using type = PackU8S; };
 
 // centre pack and its horizontal 3-neighbourhood of one row (neutral outside the image)
 template <typename T, bool SUP, typename P>
@@ -155,7 +225,7 @@ static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream
   dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(ceil_div(H, R), 256 / bx));
   if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the small-SE kernel");
   if (vec2) k_small2d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
-  else if (vec) k_small2d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  else if (vec) k_small2d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   else k_small2d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 2D kernel launch");
 }
@@ -173,7 +243,7 @@ static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W,
   dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(H, 256 / bx), (unsigned)ceil_div(D, R));
   if (grid.y > 65535 || grid.z > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "volume too large for the small-SE kernel");
   if (vec2) k_small3d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
-  else if (vec) k_small3d<T, SUP, SHAPE, Pack<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  else if (vec) k_small3d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   else k_small3d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 3D kernel launch");
 }

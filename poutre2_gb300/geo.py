@@ -134,6 +134,11 @@ class HMaximaBinaryBatch:
         _lib.call("pg_batch_plan_run", self._plan, _stream())
         _post(check)
 
+    def set_config(self, tile: int, sweeps: int):
+        """Pin the configuration instead of the autotuned one: tile 32 (register tiles) or 64
+        (shared-memory tiles), sweep sets per tile visit >= 1."""
+        _lib.call("pg_batch_plan_set_config", self._plan, int(tile), int(sweeps))
+
     @property
     def config(self):
         t, s, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -344,6 +344,52 @@ def test_batch_plan_autotuned_and_graph_replay(dt):
     plan.close()
 
 
+def _plateau_serpentine(H, W, step):
+    """A one-pixel corridor winding through the image at 100 with a 101 bump at its far end:
+    the binary h-maxima (h = 1) is 255 at the bump only once 100 has travelled the whole path."""
+    f = np.zeros((H, W), np.uint8)
+    rows = list(range(0, H, step))
+    for i, r in enumerate(rows):
+        f[r, :] = 100
+        if i + 1 < len(rows):
+            c = W - 1 if i % 2 == 0 else 0
+            f[r:rows[i + 1] + 1, c] = 100
+    last = rows[-1]
+    f[last, W - 1 if len(rows) % 2 == 0 else 0] = 101
+    return f
+
+
+@pytest.mark.parametrize("dt", TYPES)
+def test_batch_plan_pinned_configs(dt):
+    # tiles that reach the sweep cap yield and are revisited; every configuration gives the same
+    # result, including interior-only changes after a yield
+    from poutre2_gb300 import geo, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    imgs = [_plateau_serpentine(70, 45, 2), _plateau_serpentine(130, 97, 3), _plateau_serpentine(33, 64, 2),
+            synthetic.smoothed_noise_u8((90, 120), 5), synthetic.smoothed_noise_u8((1, 77), 6)]
+    imgs = [f.astype(dt) for f in imgs]
+    xs = [dev(f) for f in imgs]
+    for se in ("SECross2D", "SESquare2D"):
+        want = [oracle.h_maxima_binary(f, 1, se) for f in imgs]
+        outs = [torch.empty(x.shape, dtype=torch.uint8, device="cuda") for x in xs]
+        plan = geo.HMaximaBinaryBatch(xs, 1, Common_NL_SE[se], outs, autotune=False)
+        assert plan.config["tile"] == 32
+        tiles = (32,) if np.dtype(dt).itemsize == 8 else (32, 64)
+        for tile in tiles:
+            for sweeps in (1, 4, 512):
+                plan.set_config(tile, sweeps)
+                for o in outs:
+                    o.fill_(7)
+                plan.run(check=True)
+                for i, (w, o) in enumerate(zip(want, outs)):
+                    np.testing.assert_array_equal(host(o), w, err_msg=f"{se} tile {tile} sweeps {sweeps} image {i}")
+        with pytest.raises(Exception):
+            plan.set_config(48, 4)
+        with pytest.raises(Exception):
+            plan.set_config(32, 0)
+        plan.close()
+
+
 @pytest.mark.parametrize("dt", TYPES)
 @pytest.mark.parametrize("kind", ["low_leveling", "high_leveling", "leveling"])
 def test_leveling(dt, kind):
