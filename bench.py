@@ -425,10 +425,10 @@ def run_gpu(args):
         "parity_vs_oracle": parity,
         "e2e": {"value": ws * N / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(N), "d2h_bytes_per_step": int(N)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic_for(f"k_reconstruct@hmaxima{args.size}"),
-                     "peak_source": f"{peak_kind} hbm_gbs (burst)", "kernel": "k_reconstruct<u8,dilate,8-conn>",
+                     "traffic": traffic_for(f"k_reconstruct_wl@hmaxima{args.size}"),
+                     "peak_source": f"{peak_kind} hbm_gbs (burst)", "kernel": "k_reconstruct_wl<u8,dilate,8-conn>",
                      "algorithmic_bytes_per_launch": alg_bytes},
-        "gpu_launches": args.steps,  # one persistent k_reconstruct launch per step (plus one memset)
+        "gpu_launches": args.steps,  # one persistent k_reconstruct_wl launch per step (plus one memset)
         "clocks": clocks,
     }
     if rank == 0:

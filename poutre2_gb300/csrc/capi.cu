@@ -26,6 +26,24 @@ pg_status cuda_status(cudaError_t e, const char *what) {
   return e == cudaErrorMemoryAllocation ? PG_ERR_OUT_OF_MEMORY : PG_ERR_CUDA;
 }
 
+void retain_pool_memory() {
+  static std::mutex mu;
+  static std::vector<bool> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((size_t)dev >= done.size()) done.resize((size_t)dev + 1, false);
+  if (done[(size_t)dev]) return;
+  done[(size_t)dev] = true;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return;
+  }
+  uint64_t keep = kPoolRetainBytes;
+  if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) (void)cudaGetLastError();
+}
+
 int num_sms() {
   static std::mutex mu;
   static int cached_dev = -1, cached = 0;

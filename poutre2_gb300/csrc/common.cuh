@@ -156,6 +156,12 @@ int num_sms();
   } while (0)
 
 // Stream-ordered temporary (cudaMallocAsync / cudaFreeAsync on the call's stream).
+// Stream-ordered temporaries come from the device's default memory pool.  By default that pool
+// hands its memory back to the driver at every synchronisation, so the next call would map
+// fresh pages again; the pool keeps up to kPoolRetainBytes instead (set once per device).
+static constexpr uint64_t kPoolRetainBytes = 1ull << 30;
+void retain_pool_memory();
+
 struct Scratch {
   void *ptr = nullptr;
   cudaStream_t stream = nullptr;
@@ -163,6 +169,7 @@ struct Scratch {
   Scratch(const Scratch &) = delete;
   Scratch &operator=(const Scratch &) = delete;
   pg_status alloc(size_t bytes, cudaStream_t s) {
+    retain_pool_memory();
     stream = s;
     cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 16, s);
     if (e != cudaSuccess) {

@@ -192,7 +192,7 @@ template <typename T> __device__ __forceinline__ void st_cg(T *p, T v) {
   else __stcg(p, v);
 }
 
-enum : int { B_N = 1, B_S = 2, B_W = 4, B_E = 8, B_NW = 16, B_NE = 32, B_SW = 64, B_SE = 128, B_SELF = 256 };
+enum : int { B_N = 1, B_S = 2, B_W = 4, B_E = 8, B_NW = 16, B_NE = 32, B_SW = 64, B_SE = 128, B_SELF = 256 };  // B_x = 1 << direction
 
 // Puts the tiles next to tile (tx, ty) whose shared border changed (f: B_* bits) on the next
 // round's worklist, and the tile itself when it yielded before its local fixpoint.
@@ -216,13 +216,9 @@ __device__ void flag_neighbours(const RImg &im, unsigned *flags, int ntiles, RCt
     if (f & B_SE) flag(1, 1);
   }
   if (f & B_SELF) flag(0, 0);
-  // a changed corner pixel is also on a changed edge, so the edge bits cover every flag.  The
-  // word is read before it is written: thousands of tiles set it in a busy round, and the
-  // same-address writes would queue at one L2 slice.
-  if (f & (B_N | B_S | B_W | B_E | B_SELF)) {
-    volatile unsigned *any = &ctl->any[(round + 1) % 3];
-    if (*any == 0u) *any = 1u;
-  }
+  // a changed corner pixel is also on a changed edge, so the edge bits cover every flag.  A
+  // plain store: the writer does not wait for it (an atomic exchange would return a value).
+  if (f & (B_N | B_S | B_W | B_E | B_SELF)) *((volatile unsigned *)&ctl->any[(round + 1) % 3]) = 1u;
 }
 
 template <typename T, bool SUP, bool CONN8, int RT>
@@ -380,30 +376,88 @@ __device__ __forceinline__ const RImg &image_of(const RParams<T> &P, int tile, i
 }
 
 // Epilogue over every pixel of every image, after the last round: the binary h-maxima
-// comparison or the leveling clip by the reference.
+// comparison or the leveling clip by the reference.  Pure streaming: 16-byte vectors when the
+// image's buffers allow it, otherwise EPI_UNROLL independent elements per thread per step, so
+// that many loads are in flight (a plain grid-stride loop over single pixels would wait for
+// each load in turn).
+static constexpr int EPI_UNROLL = 8;
+
 template <typename T, bool SUP>
-__device__ void recon_epilogue(const RParams<T> &P) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int k = 0; k < P.nimg; ++k) {
-    const RImg &im = (P.nimg == 1) ? P.single : P.imgs[k];
-    const int64_t n = im.H * im.W;
-    const T *rec = static_cast<const T *>(im.rec);
-    const T *ref = static_cast<const T *>(im.mask);
-    if (P.epi == EPI_BINARY_SUP) {
-      uint8_t *o = static_cast<uint8_t *>(im.out);
-      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        o[i] = (ldg(ref + i) > ld_cg(rec + i)) ? 255 : 0;
-    } else {  // EPI_CLIP_REF: low leveling min(rec, ref), high leveling max(rec, ref)
-      T *o = static_cast<T *>(im.out);
-      for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        o[i] = Op<T, !SUP>::apply(ld_cg(rec + i), ldg(ref + i));
+__device__ __forceinline__ uint8_t epi_binary(T ref, T rec) { return ref > rec ? 255 : 0; }
+
+template <typename T, bool SUP>
+__device__ void epilogue_image(const RImg &im, int epi, int64_t tid, int64_t nth) {
+  const int64_t n = im.H * im.W;
+  const T *rec = static_cast<const T *>(im.rec);
+  const T *ref = static_cast<const T *>(im.mask);
+  constexpr int VE = 16 / (int)sizeof(T);  // pixels per 16-byte vector
+  const bool vec = ((reinterpret_cast<uintptr_t>(rec) | reinterpret_cast<uintptr_t>(ref) |
+                     reinterpret_cast<uintptr_t>(im.out)) % 16 == 0);
+  int64_t done = 0;
+  if (epi == EPI_BINARY_SUP) {
+    uint8_t *o = static_cast<uint8_t *>(im.out);
+    if (vec && sizeof(T) == 1) {
+      // 16 u8 pixels per thread and step: byte-wise unsigned compare gives 0xff / 0x00 directly
+      const int64_t nv = n / 16;
+      for (int64_t j = tid; j < nv; j += nth) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4 *>(ref) + j);
+        const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(rec) + j);
+        reinterpret_cast<uint4 *>(o)[j] =
+            make_uint4(__vcmpgtu4(a.x, b.x), __vcmpgtu4(a.y, b.y), __vcmpgtu4(a.z, b.z), __vcmpgtu4(a.w, b.w));
+      }
+      done = nv * 16;
+    }
+    for (int64_t i0 = done + tid; i0 < n; i0 += nth * EPI_UNROLL) {
+      T a[EPI_UNROLL], b[EPI_UNROLL];
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        a[u] = i < n ? ldg(ref + i) : T(0);
+        b[u] = i < n ? ld_cg(rec + i) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        if (i < n) o[i] = epi_binary<T, SUP>(a[u], b[u]);
+      }
+    }
+  } else {  // EPI_CLIP_REF: low leveling min(rec, ref), high leveling max(rec, ref)
+    T *o = static_cast<T *>(im.out);
+    if (vec) {
+      const int64_t nv = n / VE;
+      for (int64_t j = tid; j < nv; j += nth) {
+        const Pack<T> a = Pack<T>::load_cg(rec + j * VE);
+        const Pack<T> b = Pack<T>::load(ref + j * VE);
+        Pack<T>::template op<!SUP>(a, b).store(o + j * VE);
+      }
+      done = nv * VE;
+    }
+    for (int64_t i0 = done + tid; i0 < n; i0 += nth * EPI_UNROLL) {
+      T a[EPI_UNROLL], b[EPI_UNROLL];
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        a[u] = i < n ? ld_cg(rec + i) : T(0);
+        b[u] = i < n ? ldg(ref + i) : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        if (i < n) o[i] = Op<T, !SUP>::apply(a[u], b[u]);
+      }
     }
   }
 }
 
+template <typename T, bool SUP>
+__device__ void recon_epilogue(const RParams<T> &P) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  for (int k = 0; k < P.nimg; ++k) epilogue_image<T, SUP>((P.nimg == 1) ? P.single : P.imgs[k], P.epi, tid, nth);
+}
+
 template <typename T, bool SUP, bool CONN8, int RT = tile_side<T>()>
 __global__ void __launch_bounds__(RT) k_reconstruct(RParams<T> P) {
-  constexpr int RTHREADS = RT;
   constexpr int PO = tile_pitch<T>(RT + 2);
   constexpr int PM = tile_pitch<T>(RT);
   __shared__ __align__(16) T s_out[(RT + 2) * PO];
@@ -491,40 +545,12 @@ template <typename T> __device__ __forceinline__ T shfl_dn1(T v) {
   else return __shfl_down_sync(0xffffffffu, v, 1);
 }
 
-// Pixel (gy, gx) seen from a neighbouring tile: neutral outside the image, the marker in round
-// 0, the current reconstruction later.  halo_load issues the loads (at a clamped, always valid
-// address), halo_finish combines them, so that all halo loads of a visit are in flight at once.
-template <typename T> struct HaloPx {
-  T a, mk;
-  bool in;
-};
-template <typename T>
-__device__ __forceinline__ HaloPx<T> halo_load(const RImg &im, const RParams<T> &P, int round, bool need_mk,
-                                               int64_t gy, int64_t gx) {
-  HaloPx<T> h;
-  h.in = gy >= 0 && gy < im.H && gx >= 0 && gx < im.W;
-  const int64_t gi = h.in ? gy * im.W + gx : 0;
-  if (round == 0) {
-    h.a = ldg(static_cast<const T *>(im.mask) + gi);
-    h.mk = need_mk ? ldg(static_cast<const T *>(im.marker) + gi) : h.a;
-  } else {
-    h.a = ld_cg(static_cast<const T *>(im.rec) + gi);
-    h.mk = h.a;
-  }
-  return h;
-}
-template <typename T, bool SUP>
-__device__ __forceinline__ T halo_finish(const RParams<T> &P, int round, const HaloPx<T> &h) {
-  if (!h.in) return Op<T, SUP>::neutral();
-  if (round > 0) return h.a;
-  T m, v;
-  combine_init<T, SUP>(P, h.a, h.mk, m, v);
-  return v;
-}
-
+// One visit of a register tile: stage it from the reconstruction buffer (which the worklist
+// kernel's first phase set to the marker), iterate sweep sets to the tile-local fixpoint (or
+// P.max_sweeps), write it back if anything changed.  Returns the B_* bits of the borders that
+// changed (the neighbours to revisit) and B_SELF when the tile yielded.  Warp-uniform.
 template <typename T, bool SUP, bool CONN8>
-__device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_local, int round, RegS<T> *s_m,
-                                 RegS<T> *s_t) {
+__device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local, RegS<T> *s_m, RegS<T> *s_t) {
   using OS = Op<T, SUP>;   // propagation
   using OC = Op<T, !SUP>;  // clip by the mask
   const int lane = threadIdx.x & 31;
@@ -535,12 +561,29 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
   const int64_t gx = x0 + lane;
   const bool colin = gx < im.W;
 
+  // Halo loads first (they stay in flight during the stage).  Its values stay fixed during the
+  // visit, so each halo pixel's contribution is folded into one value per border pixel:
+  // `top`/`bot` per column (lane = column: the three pixels above / below), `hl`/`hr` per row
+  // (lane = row: the three pixels left / right; one in 4-connectivity).  The sweeps apply them
+  // at the tile's first/last row and column.  Addresses outside the image are clamped to pixel
+  // 0 and the values replaced by the neutral element.
+  constexpr int NH = CONN8 ? 12 : 4;
+  const int64_t hy[12] = {y0 - 1, y0 + 32, y0 + lane, y0 + lane, y0 - 1, y0 - 1, y0 + 32, y0 + 32,
+                          y0 + lane - 1, y0 + lane + 1, y0 + lane - 1, y0 + lane + 1};
+  const int64_t hx[12] = {gx, gx, x0 - 1, x0 + 32, gx - 1, gx + 1, gx - 1, gx + 1, x0 - 1, x0 - 1, x0 + 32, x0 + 32};
+  T hv[NH];
+#pragma unroll
+  for (int k = 0; k < NH; ++k) {
+    const bool in = hy[k] >= 0 && hy[k] < im.H && hx[k] >= 0 && hx[k] < im.W;
+    hv[k] = ld_cg(rec_in + (in ? hy[k] * im.W + hx[k] : 0));
+    if (!in) hv[k] = NEU;  // applied after the load returns; the load itself is unconditional
+  }
+
   // stage, lane = column: tile values and mask (pixels outside the image: neutral, fixed).
-  // Loads come first, 16 rows at a time, so that they are all in flight together; the
-  // addresses of pixels outside the image are clamped to pixel 0 and the values discarded.
+  // Loads come first, 16 rows at a time, so that they are all in flight together.
   const T *mk_in = static_cast<const T *>(im.marker);
   const T *ms_in = static_cast<const T *>(im.mask);
-  const bool need_mk = needs_marker(P, round);
+  const bool need_mk = needs_marker(P, 1);
   T v[32];
 #pragma unroll
   for (int h = 0; h < 32; h += 16) {
@@ -551,14 +594,12 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
       const int64_t gi = (colin && gy < im.H) ? gy * im.W + gx : 0;
       a[r] = ldg(ms_in + gi);
       b[r] = need_mk ? ldg(mk_in + gi) : a[r];
-      if (round > 0) v[h + r] = ld_cg(rec_in + gi);
+      v[h + r] = ld_cg(rec_in + gi);
     }
 #pragma unroll
     for (int r = 0; r < 16; ++r) {
       const bool ok = colin && y0 + h + r < im.H;
-      T m;
-      if (round == 0) combine_init<T, SUP>(P, a[r], b[r], m, v[h + r]);
-      else m = combine_mask(P, a[r], b[r]);
+      T m = combine_mask(P, a[r], b[r]);
       if (!ok) {
         m = NEU;
         v[h + r] = NEU;
@@ -566,37 +607,12 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
       s_m[(h + r) * kRP + lane] = m;
     }
   }
-  // Halo.  Its values stay fixed during the visit, so each halo pixel's contribution is
-  // folded into one value per border pixel: `top`/`bot` per column (lane = column: the three
-  // pixels above / below), `hl`/`hr` per row (lane = row: the three pixels left / right; one
-  // in 4-connectivity).  The sweeps apply them at the tile's first/last row and column.
-  T top, bot, hl, hr;
-  {
-    HaloPx<T> q[12];
-    q[0] = halo_load(im, P, round, need_mk, y0 - 1, gx);
-    q[1] = halo_load(im, P, round, need_mk, y0 + 32, gx);
-    q[2] = halo_load(im, P, round, need_mk, y0 + lane, x0 - 1);
-    q[3] = halo_load(im, P, round, need_mk, y0 + lane, x0 + 32);
-    if (CONN8) {
-      q[4] = halo_load(im, P, round, need_mk, y0 - 1, gx - 1);
-      q[5] = halo_load(im, P, round, need_mk, y0 - 1, gx + 1);
-      q[6] = halo_load(im, P, round, need_mk, y0 + 32, gx - 1);
-      q[7] = halo_load(im, P, round, need_mk, y0 + 32, gx + 1);
-      q[8] = halo_load(im, P, round, need_mk, y0 + lane - 1, x0 - 1);
-      q[9] = halo_load(im, P, round, need_mk, y0 + lane + 1, x0 - 1);
-      q[10] = halo_load(im, P, round, need_mk, y0 + lane - 1, x0 + 32);
-      q[11] = halo_load(im, P, round, need_mk, y0 + lane + 1, x0 + 32);
-    }
-    top = halo_finish<T, SUP>(P, round, q[0]);
-    bot = halo_finish<T, SUP>(P, round, q[1]);
-    hl = halo_finish<T, SUP>(P, round, q[2]);
-    hr = halo_finish<T, SUP>(P, round, q[3]);
-    if (CONN8) {
-      top = OS::apply(top, OS::apply(halo_finish<T, SUP>(P, round, q[4]), halo_finish<T, SUP>(P, round, q[5])));
-      bot = OS::apply(bot, OS::apply(halo_finish<T, SUP>(P, round, q[6]), halo_finish<T, SUP>(P, round, q[7])));
-      hl = OS::apply(hl, OS::apply(halo_finish<T, SUP>(P, round, q[8]), halo_finish<T, SUP>(P, round, q[9])));
-      hr = OS::apply(hr, OS::apply(halo_finish<T, SUP>(P, round, q[10]), halo_finish<T, SUP>(P, round, q[11])));
-    }
+  T top = hv[0], bot = hv[1], hl = hv[2], hr = hv[3];
+  if (CONN8) {
+    top = OS::apply(top, OS::apply(hv[4], hv[5]));
+    bot = OS::apply(bot, OS::apply(hv[6], hv[7]));
+    hl = OS::apply(hl, OS::apply(hv[8], hv[9]));
+    hr = OS::apply(hr, OS::apply(hv[10], hv[11]));
   }
   // staged borders, to tell afterwards which neighbours must be revisited
 #pragma unroll
@@ -609,32 +625,34 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
   bool converged = false, changed = false, wch = false, ech = false;
   for (int sweep = 0; sweep < P.max_sweeps; ++sweep) {
     bool ch = false;
-    // down: the row above (lane 0 / 31 get their own value back from the shuffle: the pixels
-    // beyond the tile's side columns are halo, applied by the horizontal sweeps)
-#pragma unroll
-    for (int r = 0; r < 32; ++r) {
-      T nb;
-      if (r == 0) nb = top;
-      else {
-        nb = v[r - 1];
-        if (CONN8) nb = OS::apply(nb, OS::apply(shfl_up1(nb), shfl_dn1(nb)));
-      }
+    auto vstep = [&](int r, T nb) {
       const T nv = OC::apply(OS::apply(v[r], nb), lds_mask<T>(s_m + r * kRP + lane));
       ch |= nv != v[r];
       v[r] = nv;
+    };
+    // the three pixels of a row seen from the row below / above (lanes 0 and 31 get their own
+    // value back from the shuffle: the pixels beyond the tile's sides are halo, applied by the
+    // horizontal sweeps)
+    auto nbrow = [&](T p) -> T {
+      if (CONN8) return OS::apply(p, OS::apply(shfl_up1(p), shfl_dn1(p)));
+      return p;
+    };
+    // vertical, two independent chains at once: down over the top half with up over the
+    // bottom half, then down over the bottom half with up over the top half.  A value still
+    // travels the whole column in one direction per sweep set.
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const T nd = (k == 0) ? top : nbrow(v[k - 1]);
+      const T nu = (k == 0) ? bot : nbrow(v[32 - k]);
+      vstep(k, nd);
+      vstep(31 - k, nu);
     }
-    // up: the row below
 #pragma unroll
-    for (int r = 31; r >= 0; --r) {
-      T nb;
-      if (r == 31) nb = bot;
-      else {
-        nb = v[r + 1];
-        if (CONN8) nb = OS::apply(nb, OS::apply(shfl_up1(nb), shfl_dn1(nb)));
-      }
-      const T nv = OC::apply(OS::apply(v[r], nb), lds_mask<T>(s_m + r * kRP + lane));
-      ch |= nv != v[r];
-      v[r] = nv;
+    for (int k = 0; k < 16; ++k) {
+      const T nd = nbrow(v[15 + k]);
+      const T nu = nbrow(v[16 - k]);
+      vstep(16 + k, nd);
+      vstep(15 - k, nu);
     }
     // to lane = row
 #pragma unroll
@@ -643,22 +661,21 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
 #pragma unroll
     for (int c = 0; c < 32; ++c) v[c] = (T)s_t[lane * kRP + c];
     __syncwarp();
-    // right: the pixel on the left; left: the pixel on the right
-    T prev = hl;
-#pragma unroll
-    for (int c = 0; c < 32; ++c) {
-      const T nv = OC::apply(OS::apply(v[c], prev), lds_mask<T>(s_m + lane * kRP + c));
+    // horizontal (the pixel on the left / on the right), two chains at once in the same way
+    auto hstep = [&](int c, T nb) {
+      const T nv = OC::apply(OS::apply(v[c], nb), lds_mask<T>(s_m + lane * kRP + c));
       ch |= nv != v[c];
       v[c] = nv;
-      prev = nv;
+    };
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      hstep(k, k == 0 ? hl : v[k - 1]);
+      hstep(31 - k, k == 0 ? hr : v[32 - k]);
     }
-    prev = hr;
 #pragma unroll
-    for (int c = 31; c >= 0; --c) {
-      const T nv = OC::apply(OS::apply(v[c], prev), lds_mask<T>(s_m + lane * kRP + c));
-      ch |= nv != v[c];
-      v[c] = nv;
-      prev = nv;
+    for (int k = 0; k < 16; ++k) {
+      hstep(16 + k, v[15 + k]);
+      hstep(15 - k, v[16 - k]);
     }
     wch = v[0] != initL;
     ech = v[31] != initR;
@@ -690,7 +707,7 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
   if (bS & 1u) f |= B_SW;
   if (bS >> 31) f |= B_SE;
 
-  if (round == 0 || changed) {
+  if (changed) {
     // the row stride goes through a shuffle so that the compiler recomputes these addresses
     // here instead of keeping the stage's 32 row addresses alive across the sweeps
     const long long Wd = __shfl_sync(0xffffffffu, (long long)im.W, 0);
@@ -701,65 +718,296 @@ __device__ void process_tile_reg(const RImg &im, const RParams<T> &P, int t_loca
       p += Wd;
     }
   }
-  if (lane == 0 && f != 0) flag_neighbours<CONN8>(im, P.flags, P.ntiles, P.ctl, round, tx, ty, f);
-  __syncwarp();
+  return f;
 }
 
+// ------------------------------------------------------------------ tile worklist
+// The register-tile kernel has no rounds.  Every tile is queued once at the start; a warp pops
+// a tile, visits it, and queues the neighbours whose shared border changed.  The kernel ends
+// when no tile is queued or being visited (`pending` == 0).  A tile is visited by one warp at a
+// time, through its state:
+//   IDLE --queue--> QUEUED --pop--> RUNNING --done--> IDLE (or QUEUED again if it yielded)
+//   RUNNING --a neighbour changed its border meanwhile--> DIRTY --done--> QUEUED
+// The queue is a ring of 64-bit slots (position tag << 32 | tile + 1), a multi-producer multi-
+// consumer ring with sequence numbers: a popper takes a ticket with one atomicAdd on `head`
+// and waits for its slot to carry its position; a pusher takes positions with one atomicAdd
+// on `tail` and waits until the slot's previous lap was consumed (tag = position - cap, tile
+// field 0).  No compare-and-swap retries on the shared counters.
+enum : unsigned { TS_IDLE = 0, TS_QUEUED = 1, TS_RUNNING = 2, TS_DIRTY = 3 };
+
+struct RQueue {             // each counter on its own 128-byte line
+  unsigned head, pad0[31];  // next ticket to pop
+  unsigned tail, pad1[31];  // next position to push
+  int pending, pad2[31];    // tiles queued or being visited
+  unsigned pad3[32];
+};
+static_assert(sizeof(RQueue) == 512, "RQueue layout");
+
+template <typename T> struct WorkList {
+  RQueue *q;
+  unsigned *state;             // ntiles
+  unsigned long long *ring;    // cap slots
+  unsigned cap;
+};
+
+__device__ __forceinline__ bool wait_expired(RCtl *ctl, unsigned long long t0) {
+  if (global_ns() - t0 > kBarrierTimeoutNs) {
+    set_status(ctl, PG_ERR_NOT_CONVERGED);
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ unsigned long long slot_val(unsigned pos, unsigned tile1) {
+  return ((unsigned long long)pos << 32) | tile1;
+}
+
+// Lane 0 pops: the tile to visit, or -1 when the work is done or an error was recorded.
+template <typename T>
+__device__ int wl_pop(const WorkList<T> &wl, RCtl *ctl, long long max_tickets) {
+  const unsigned pos = atomicAdd(&wl.q->head, 1u);
+  if ((long long)pos >= max_tickets) {  // runaway guard: far more visits than any input needs
+    set_status(ctl, PG_ERR_NOT_CONVERGED);
+    return -1;
+  }
+  volatile unsigned long long *slot = wl.ring + pos % wl.cap;
+  const unsigned long long t0 = global_ns();
+  unsigned ns = 32;
+  unsigned long long v;
+  for (;;) {
+    v = *slot;
+    if ((unsigned)(v >> 32) == pos && (unsigned)v != 0u) break;
+    if (*((volatile int *)&wl.q->pending) == 0) return -1;
+    if (*((volatile int *)&ctl->status) != 0) return -1;
+    __nanosleep(ns);
+    if (ns < 4096) ns <<= 1;
+    if (wait_expired(ctl, t0)) return -1;
+  }
+  *slot = slot_val(pos, 0u);  // consumed: the next lap's pusher may write
+  const unsigned tile = (unsigned)v - 1u;
+  *((volatile unsigned *)(wl.state + tile)) = TS_RUNNING;  // QUEUED until now: nobody else moves it
+  __threadfence();  // the neighbours' pixels written before they queued this tile
+  return (int)tile;
+}
+
+// Retry limit of the state-change loops below: a retry means another warp changed the same
+// word in between, which happens a bounded number of times; the limit only guards the kernel.
+static constexpr int kCasRetries = 1 << 20;
+
+// Warp-wide end of a visit: lanes 0..7 queue the neighbours whose shared border changed (one
+// lane each, in parallel), lane 8 releases the tile (or queues it again), and the queued tiles
+// are pushed with one position reservation for the warp.  Called by the whole warp.
+// (Keeping one queued neighbour as the warp's next visit, past the ring, was measured: it
+// shortens long propagations but makes tiles of short ones -- the h-extrema -- be revisited
+// more often, so every queued tile goes through the ring.)
+template <typename T, bool CONN8>
+__device__ void wl_finish(const WorkList<T> &wl, RCtl *ctl, const RImg &im, int tile, int t_local, int f) {
+  const int lane = threadIdx.x & 31;
+  const int tx = t_local % im.tiles_x, ty = t_local / im.tiles_x;
+  // lane d < 8 handles direction d = N S W E NW NE SW SE, whose B_* bit is 1 << d
+  int cand = -1;
+  bool push = false;
+  if (lane < (CONN8 ? 8 : 4) && (f & (1 << lane))) {
+    const int dx = lane < 2 ? 0 : ((lane & 1) ? 1 : -1);
+    const int dy = lane < 2 ? (lane ? 1 : -1) : lane < 4 ? 0 : (lane < 6 ? -1 : 1);
+    const int nx = tx + dx, ny = ty + dy;
+    if (nx >= 0 && ny >= 0 && nx < im.tiles_x && ny < im.tiles_y) cand = im.tile_begin + ny * im.tiles_x + nx;
+  }
+  if (cand >= 0) {
+    bool done = false;
+    for (int it = 0; it < kCasRetries && !done; ++it) {
+      const unsigned s = atomicCAS(wl.state + cand, TS_IDLE, TS_QUEUED);
+      if (s == TS_IDLE) push = done = true;
+      else if (s != TS_RUNNING) done = true;  // already queued, or already marked for another visit
+      else if (atomicCAS(wl.state + cand, TS_RUNNING, TS_DIRTY) == TS_RUNNING) done = true;
+    }
+    if (!done) set_status(ctl, PG_ERR_NOT_CONVERGED);
+  }
+  if (lane == 8) {
+    // release: back to IDLE, or queued again if it yielded or a neighbour changed meanwhile
+    const bool yielded = (f & B_SELF) != 0;
+    bool done = false;
+    for (int it = 0; it < kCasRetries && !done; ++it) {
+      const unsigned s = *((volatile unsigned *)(wl.state + tile));  // RUNNING or DIRTY: only we move it out
+      if (s == TS_DIRTY || yielded) {
+        if (atomicCAS(wl.state + tile, s, TS_QUEUED) == s) push = done = true;
+      } else if (atomicCAS(wl.state + tile, TS_RUNNING, TS_IDLE) == TS_RUNNING) {
+        done = true;
+      }
+    }
+    if (!done) set_status(ctl, PG_ERR_NOT_CONVERGED);
+    cand = tile;
+  }
+  const unsigned pm = __ballot_sync(0xffffffffu, push);
+  const int n = __popc(pm);
+  unsigned base = 0;
+  if (lane == 0 && n > 0) {
+    atomicAdd(&wl.q->pending, n);
+    base = atomicAdd(&wl.q->tail, (unsigned)n);
+  }
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (push) {
+    const unsigned pos = base + __popc(pm & ((1u << lane) - 1u));
+    volatile unsigned long long *slot = wl.ring + pos % wl.cap;
+    const unsigned long long want = slot_val(pos - wl.cap, 0u);  // previous lap consumed
+    const unsigned long long t0 = global_ns();
+    while (*slot != want) {
+      __nanosleep(64);
+      if (wait_expired(ctl, t0)) break;
+    }
+    *slot = slot_val(pos, (unsigned)cand + 1u);
+  }
+  if (lane == 0) atomicSub(&wl.q->pending, 1);  // after this warp's pushes were counted: never 0 early
+}
+
+// first phase: every reconstruction buffer starts at the marker (select_marker, or the
+// saturated shift of the h-extrema), EPI_UNROLL pixels per thread and step
+template <typename T, bool SUP>
+__device__ void init_rec(const RParams<T> &P, int64_t tid, int64_t nth) {
+  const bool need_mk = needs_marker(P, 0);
+  for (int k = 0; k < P.nimg; ++k) {
+    const RImg &im = (P.nimg == 1) ? P.single : P.imgs[k];
+    const int64_t n = im.H * im.W;
+    const T *ms = static_cast<const T *>(im.mask);
+    const T *mk = static_cast<const T *>(im.marker);
+    T *rec = static_cast<T *>(im.rec);
+    for (int64_t i0 = tid; i0 < n; i0 += nth * EPI_UNROLL) {
+      T a[EPI_UNROLL], b[EPI_UNROLL];
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        a[u] = i < n ? ldg(ms + i) : T(0);
+        b[u] = (need_mk && i < n) ? ldg(mk + i) : a[u];
+      }
+#pragma unroll
+      for (int u = 0; u < EPI_UNROLL; ++u) {
+        const int64_t i = i0 + u * nth;
+        T m, v;
+        combine_init<T, SUP>(P, a[u], b[u], m, v);
+        if (i < n) st_cg(rec + i, v);
+      }
+    }
+  }
+}
+
+__device__ long long g_recon_visits = 0;
+
 template <typename T, bool SUP, bool CONN8>
-__global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_reg(RParams<T> P) {
+__global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T> P, WorkList<T> wl) {
   static_assert(sizeof(T) <= 4, "register tiles hold pixels of at most 4 bytes");
   __shared__ RegS<T> s_m[kRegWarps][32 * kRP];
   __shared__ RegS<T> s_t[kRegWarps][32 * kRP];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   RCtl *ctl = P.ctl;
-  const int wstride = gridDim.x * kRegWarps;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
 
-  int round = 0;
-  bool ok = true;
+  // phase 0: marker into the reconstruction buffers, every tile queued once
+  init_rec<T, SUP>(P, tid, nth);
+  for (int64_t i = tid; i < (int64_t)wl.cap; i += nth) {
+    // positions 0..ntiles-1 hold the tiles; the others wait for their first lap
+    wl.ring[i] = i < P.ntiles ? slot_val((unsigned)i, (unsigned)i + 1u) : slot_val((unsigned)i - wl.cap, 0u);
+    if (i < P.ntiles) wl.state[i] = TS_QUEUED;
+  }
+  if (tid == 0) {
+    wl.q->tail = (unsigned)P.ntiles;
+    wl.q->pending = P.ntiles;
+  }
+  if (!grid_barrier(ctl)) return;
+
+  // phase 1: visits until no tile is queued or running
+  // runaway guard on the tickets (visits plus idle pops), also below the wrap of the 32-bit ring
+  // positions
+  const long long max_tickets = std::min<long long>((long long)P.ntiles * P.max_rounds, (1ll << 31) - 2ll * P.ntiles);
   for (;;) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->any[(round + 2) % 3] = 0u;
-    unsigned *fcur = P.flags + (size_t)(round & 1) * P.ntiles;
-    for (int t = blockIdx.x * kRegWarps + warp; t < P.ntiles; t += wstride) {
-      int a = 1;
-      if (round > 0) {
-        if (lane == 0) {
-          a = *((volatile unsigned *)(fcur + t)) != 0u;
-          if (a) fcur[t] = 0u;
-        }
-        a = __shfl_sync(0xffffffffu, a, 0);
-      }
-      if (a) {
-        int tl = 0;
-        const RImg &im = image_of(P, t, tl);
-        process_tile_reg<T, SUP, CONN8>(im, P, tl, round, s_m[warp], s_t[warp]);
-      }
-    }
-    if (!grid_barrier(ctl)) { ok = false; break; }
-    const unsigned any = *((volatile unsigned *)&ctl->any[(round + 1) % 3]);
-    ++round;
-    if (!any) break;
-    if (round >= P.max_rounds) {
-      if (threadIdx.x == 0) set_status(ctl, PG_ERR_NOT_CONVERGED);
-      ok = false;
-      break;
-    }
+    int t = -1;
+    if (lane == 0) t = wl_pop(wl, ctl, max_tickets);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t < 0) break;
+    int tl = 0;
+    const RImg &im = image_of(P, t, tl);
+    const int f = process_tile_reg<T, SUP, CONN8>(im, P, tl, s_m[warp], s_t[warp]);
+    __threadfence();  // this tile's pixels, before any neighbour is queued
+    __syncwarp();
+    wl_finish<T, CONN8>(wl, ctl, im, t, tl, f);
+    __syncwarp();
   }
+  if (!grid_barrier(ctl)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->rounds = round;
-    g_recon_rounds = round;
+    const long long visits = (long long)*((volatile unsigned *)&wl.q->tail);  // every pushed tile was visited
+    g_recon_visits = visits;
+    g_recon_rounds = (int)((visits + P.ntiles - 1) / P.ntiles);
+    ctl->rounds = g_recon_rounds;
   }
-  if (!ok || P.epi == EPI_NONE) return;
+  if (P.epi == EPI_NONE) return;
   recon_epilogue<T, SUP>(P);
 }
 
 // ------------------------------------------------------------------ host side
+// Scratch work area of one launch: control block (256 B) | worklist counters (512 B) | per-tile
+// words: the double-buffered flags of the round kernel, or the tile states and the ring of the
+// worklist.  The work area is cleared before the launch.
+static constexpr size_t kWorkHead = 256 + sizeof(RQueue);
+static unsigned ring_cap(int64_t ntiles) { return (unsigned)(2 * ntiles + 4096); }
+static size_t ring_offset(int64_t ntiles) { return ((4 * (size_t)ntiles + 255) / 256) * 256; }
+static size_t work_bytes(int64_t ntiles) {
+  return kWorkHead + ring_offset(ntiles) + ((8 * (size_t)ring_cap(ntiles) + 255) / 256) * 256;
+}
+
+// Launches the reconstruction kernel for tile side RT: the worklist kernel on register tiles
+// for 32-pixel tiles of pixels up to 4 bytes, the round kernel on shared-memory tiles otherwise.
+// P's images, tiles and modes are set by the caller; `work` is a cleared work area.
+template <typename T, bool SUP, bool CONN8, int RT>
+static pg_status launch_recon(RParams<T> &P, char *work, cudaStream_t s, int *grid_out) {
+  constexpr bool REG = RT == 32 && sizeof(T) <= 4;
+  constexpr int THREADS = REG ? kRegWarps * 32 : RT;
+  constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
+  P.ctl = reinterpret_cast<RCtl *>(work);
+  P.flags = reinterpret_cast<unsigned *>(work + kWorkHead);
+  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)P.ntiles);
+  WorkList<T> wl{};
+  wl.q = reinterpret_cast<RQueue *>(work + 256);
+  wl.state = P.flags;
+  wl.ring = reinterpret_cast<unsigned long long *>(work + kWorkHead + ring_offset(P.ntiles));
+  wl.cap = ring_cap(P.ntiles);
+  void *kern = nullptr;
+  if constexpr (REG) kern = reinterpret_cast<void *>(k_reconstruct_wl<T, SUP, CONN8>);
+  else kern = reinterpret_cast<void *>(k_reconstruct<T, SUP, CONN8, RT>);
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  static std::mutex mu;
+  static std::vector<int> cached;  // blocks per SM, per device
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if ((size_t)dev >= cached.size()) cached.resize((size_t)dev + 1, 0);
+    if (cached[(size_t)dev] == 0)
+      PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached[(size_t)dev], kern, THREADS, 0), "occupancy");
+    per_sm = cached[(size_t)dev];
+  }
+  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
+  int grid = per_sm * num_sms();
+  if (grid > ceil_div(P.ntiles, TILES_PER_CTA)) grid = (int)ceil_div(P.ntiles, TILES_PER_CTA);
+  if (grid_out) *grid_out = grid;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if constexpr (REG) PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_reconstruct_wl<T, SUP, CONN8>, P, wl), "cooperative reconstruction launch");
+  else PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_reconstruct<T, SUP, CONN8, RT>, P), "cooperative reconstruction launch");
+  return PG_OK;
+}
+
 template <typename T, bool SUP, bool CONN8>
 static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool binary, cudaStream_t s) {
   // register tiles (32x32, a warp each) up to 4-byte pixels, shared-memory tiles for 8-byte ones
-  constexpr bool REG = sizeof(T) <= 4;
-  constexpr int RT = REG ? 32 : tile_side<T>();
-  constexpr int RTHREADS = REG ? kRegWarps * 32 : RT;
-  constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
+  constexpr int RT = sizeof(T) <= 4 ? 32 : tile_side<T>();
   int ntiles = 0;
   size_t rec_bytes = 0;
   for (auto &im : imgs) {
@@ -771,9 +1019,8 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   }
   if (ntiles == 0) return PG_OK;
   const int nimg = (int)imgs.size();
-  // scratch: control block | flags | image table | reconstruction buffers (binary mode)
-  const size_t off_flags = 256;
-  const size_t off_tab = off_flags + ((sizeof(unsigned) * 2 * (size_t)ntiles + 255) / 256) * 256;
+  // scratch: work area | image table | reconstruction buffers (binary mode)
+  const size_t off_tab = work_bytes(ntiles);
   const size_t off_rec = off_tab + ((sizeof(RImg) * (size_t)(nimg > 1 ? nimg : 0) + 255) / 256) * 256;
   const size_t total = off_rec + rec_bytes + 256;
   Scratch scr;
@@ -787,7 +1034,7 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
       off = (off + 15) / 16 * 16;
     }
   }
-  PG_CUDA_TRY(cudaMemsetAsync(base, 0, off_tab, s), "clear reconstruction control block");
+  PG_CUDA_TRY(cudaMemsetAsync(base, 0, off_tab, s), "clear reconstruction work area");
   std::vector<RImg> table;
   if (nimg > 1) {
     table = imgs;
@@ -799,49 +1046,11 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   P.imgs = reinterpret_cast<const RImg *>(base + off_tab);
   P.nimg = nimg;
   P.ntiles = ntiles;
-  P.ctl = reinterpret_cast<RCtl *>(base);
-  P.flags = reinterpret_cast<unsigned *>(base + off_flags);
-  // A round moves information across at least one tile border, so the rounds needed are
-  // bounded by the tile crossings of the longest geodesic path; the cap only guards against
-  // a runaway (termination is guaranteed: every round raises some pixel to another input value).
-  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)ntiles);
   P.init = rq.init;
   P.mask_mode = rq.mask_mode;
   P.epi = rq.epi;
   P.h = static_cast<T>(rq.h);
-
-  void (*kern)(RParams<T>) = nullptr;
-  if constexpr (REG) kern = k_reconstruct_reg<T, SUP, CONN8>;
-  else kern = k_reconstruct<T, SUP, CONN8>;
-  int dev = 0;
-  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
-  static std::mutex mu;
-  static int cached_dev = -1, cached_blocks = 0;
-  int per_sm = 0;
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    if (cached_dev != dev) {
-      PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cached_blocks, kern, RTHREADS, 0), "occupancy");
-      cached_dev = dev;
-    }
-    per_sm = cached_blocks;
-  }
-  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
-  int grid = per_sm * num_sms();
-  if (grid > ceil_div(ntiles, TILES_PER_CTA)) grid = (int)ceil_div(ntiles, TILES_PER_CTA);
-
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(RTHREADS);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P), "cooperative reconstruction launch");
-  return PG_OK;
+  return launch_recon<T, SUP, CONN8, RT>(P, base, s, nullptr);
 }
 
 template <typename T>
@@ -914,39 +1123,13 @@ static pg_status plan_launch_t(pg_batch_plan &p, int sweeps, cudaStream_t s, int
   P.imgs = tb.d_imgs;
   P.nimg = (int)tb.imgs.size();
   P.ntiles = tb.ntiles;
-  P.ctl = static_cast<RCtl *>(p.scratch);
-  P.flags = reinterpret_cast<unsigned *>(static_cast<char *>(p.scratch) + 256);
-  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)tb.ntiles);
   P.max_sweeps = sweeps;
   P.init = INIT_SAT_CONST;
   P.mask_mode = MASK_PLAIN;
   P.epi = EPI_BINARY_SUP;
   P.h = static_cast<T>(p.h);
-  // 32-pixel tiles of pixels up to 4 bytes run as register tiles (a warp per tile)
-  constexpr bool REG = RT == 32 && sizeof(T) <= 4;
-  constexpr int THREADS = REG ? kRegWarps * 32 : RT;
-  constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
-  void (*kern)(RParams<T>) = nullptr;
-  if constexpr (REG) kern = k_reconstruct_reg<T, true, CONN8>;
-  else kern = k_reconstruct<T, true, CONN8, RT>;
-  int per_sm = 0;
-  PG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, 0), "occupancy");
-  if (per_sm < 1) return fail(PG_ERR_CUDA, "reconstruction kernel cannot be resident");
-  int grid = per_sm * num_sms();
-  if (grid > ceil_div(tb.ntiles, TILES_PER_CTA)) grid = (int)ceil_div(tb.ntiles, TILES_PER_CTA);
-  if (grid_out) *grid_out = grid;
-  PG_CUDA_TRY(cudaMemsetAsync(p.scratch, 0, p.clear_bytes, s), "clear batch worklist");
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(THREADS);
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  PG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P), "cooperative batch launch");
-  return PG_OK;
+  PG_CUDA_TRY(cudaMemsetAsync(p.scratch, 0, p.clear_bytes, s), "clear batch work area");
+  return launch_recon<T, true, CONN8, RT>(P, static_cast<char *>(p.scratch), s, grid_out);
 }
 
 template <typename T>
@@ -1007,9 +1190,7 @@ pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, do
   plan_tables(*plan, base, 64, plan->t64);
   plan_tables(*plan, base, 32, plan->t32);
   const int max_tiles = std::max(plan->t64.ntiles, plan->t32.ntiles);
-  const size_t off_flags = 256;
-  const size_t flags_bytes = ((sizeof(unsigned) * 2 * (size_t)max_tiles + 255) / 256) * 256;
-  const size_t off_tab64 = off_flags + flags_bytes;
+  const size_t off_tab64 = work_bytes(max_tiles);
   const size_t tab_bytes = ((sizeof(RImg) * (size_t)n + 255) / 256) * 256;
   const size_t off_tab32 = off_tab64 + tab_bytes;
   size_t off_rec = off_tab32 + tab_bytes;
