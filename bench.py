@@ -194,8 +194,9 @@ def _time_ms(fn, flush, reps=5, warm=2):
     return statistics.median(out)
 
 
-def extra_measurements(dev, flush):
-    """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way."""
+def extra_measurements(dev, flush, only=None):
+    """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
+    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5), or all."""
     import numpy as np
     import torch
 
@@ -320,7 +321,8 @@ def extra_measurements(dev, flush):
             del xr
 
     for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5):
-        guard(fn)
+        if only is None or fn.__name__ in only:
+            guard(fn)
     return res
 
 
@@ -438,7 +440,8 @@ def run_gpu(args):
                                     "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
                                               f"(poutre2 is single-threaded)"}
         if args.extra:
-            line["extra"] = extra_measurements(dev, flush)
+            only = set(args.only.split(",")) if args.only else None
+            line["extra"] = extra_measurements(dev, flush, only)
         print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()
@@ -456,6 +459,7 @@ def main():
     ap.add_argument("--extra", action="store_true", default=True, help="also measure the other workloads (default)")
     ap.add_argument("--no-extra", dest="extra", action="store_false")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--only", default="", help="comma-separated subset of the extra workloads (e.g. cfg3,cfg5)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

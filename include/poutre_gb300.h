@@ -245,8 +245,9 @@ PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker,
  * to observe the failure the reference would have thrown. */
 PG_API pg_status pg_check_device(pg_stream_t stream);
 
-/* Number of persistent rounds the last completed reconstruction on the current device needed
- * (diagnostics; synchronises the device). */
+/* Passes of the last completed reconstruction on the current device (diagnostics; synchronises
+ * the device): for the shared-memory tile kernel the rounds of tile visits, for the worklist kernel
+ * (pixels of at most 4 bytes) the tile visits divided by the number of tiles, rounded up. */
 PG_API int32_t pg_last_reconstruction_rounds(void);
 
 #ifdef __cplusplus
