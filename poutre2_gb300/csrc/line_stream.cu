@@ -1,8 +1,10 @@
-// line_stream.cu -- register-streaming vertical segments (van Herk / Gil-Werman in registers).
+// line_stream.cu -- register-streaming vertical and diagonal segments (van Herk / Gil-Werman in
+// registers).
 //
 // Same result as line.cu / line_w.cu for the Y segment of 2K+1 pixels (DilateY/ErodeY,
-// ero_dil_line_se_t.hpp:249-282; clipped window).  Used for the half lengths instantiated
-// below, 1/2/4-byte pixels, word-aligned rows.
+// ero_dil_line_se_t.hpp:249-282; clipped window) and for the 45 / 135 degree segments (runtime
+// neighbour lists).  Used for the half lengths instantiated below, 1/2/4-byte pixels, word-aligned
+// rows.
 //
 // A thread owns one 32-bit word column (E = 4/sizeof(T) adjacent pixel columns) of a strip of
 // rows and walks down it block by block (blocks of W = 2K+1 rows, anchored K rows above the
@@ -58,6 +60,59 @@ __global__ void __launch_bounds__(kLSThreads) k_vline_stream(const uint32_t *__r
   }
 }
 
+// Diagonal segments, same scheme along a diagonal, one pixel per thread: lane j of a warp follows
+// the diagonal through pixel x0 + j of row y0, i.e. x(y) = x0 + j - d (45 degrees: x + y constant)
+// or x0 + j + d (135 degrees: x - y constant), d = y - y0.  A warp's 32 pixels of a row are
+// contiguous, so loads and stores stay coalesced (unaligned by the row's shift); pixels outside
+// the image read as neutral and are not written.  Packing several pixels per word would make each
+// lane's word unaligned by a row-dependent shift and need a shuffle per row; measured slower.
+template <typename T, bool SUP, int K, int DIR>  // DIR = +1: 45 degrees (dx = -1), -1: 135 degrees (dx = +1)
+__global__ void __launch_bounds__(kLSThreads) k_dline_stream(const T *__restrict__ in, T *__restrict__ out, int H,
+                                                            int Wd, int strip, int x_first) {
+  constexpr int W = 2 * K + 1;
+  const int x0 = x_first + blockIdx.x * kLSThreads + threadIdx.x;  // this thread's pixel at row y0
+  const int y0 = blockIdx.y * strip;
+  const int y1 = min(y0 + strip, H);
+  const T NEU = Op<T, SUP>::neutral();
+  T suf[W];
+#pragma unroll
+  for (int i = 0; i < W; ++i) suf[i] = NEU;
+  const int ys = y0 - K;
+  for (int yb = ys; yb < y1 + K; yb += W) {
+    T raw[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int y = yb + i;
+      const int x = DIR > 0 ? x0 - (y - y0) : x0 + (y - y0);
+      raw[i] = (y >= 0 && y < H && x >= 0 && x < Wd) ? ldg(in + (size_t)y * Wd + x) : NEU;
+    }
+    T pre = raw[0];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0) pre = Op<T, SUP>::apply(pre, raw[i]);
+      const int y = yb + i - K;
+      const int x = DIR > 0 ? x0 - (y - y0) : x0 + (y - y0);
+      if (y >= y0 && y < y1 && x >= 0 && x < Wd)
+        out[(size_t)y * Wd + x] = (i < W - 1) ? Op<T, SUP>::apply(suf[i + 1], pre) : pre;
+    }
+    suf[W - 1] = raw[W - 1];
+#pragma unroll
+    for (int i = W - 2; i >= 0; --i) suf[i] = Op<T, SUP>::apply(suf[i + 1], raw[i]);
+  }
+}
+
+template <typename T, bool SUP, int K, int DIR>
+static void ds_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
+  // threads cover W + strip pixels of row y0: the band drifts left (45) or right (135) by one pixel
+  // per row over the strip
+  int strip = 256;
+  auto ctas_x = [&](int st) { return ceil_div((int64_t)W + st, kLSThreads); };
+  while (strip > 32 && ctas_x(strip) * ceil_div(H, strip) < 4LL * num_sms()) strip /= 2;
+  const int x_first = DIR > 0 ? 0 : -strip;
+  dim3 grid((unsigned)ctas_x(strip), (unsigned)ceil_div(H, strip));
+  k_dline_stream<T, SUP, K, DIR><<<grid, kLSThreads, 0, s>>>(in, out, H, W, strip, x_first);
+}
+
 template <typename T, bool SUP, int K>
 static void vs_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
   constexpr int E = 4 / (int)sizeof(T);
@@ -71,53 +126,65 @@ static void vs_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
                                                        reinterpret_cast<uint32_t *>(out), H, Wn, strip);
 }
 
+template <typename T, bool SUP, int K>
+static void line_launch(const T *in, T *out, int H, int W, int dx, cudaStream_t s) {
+  if (dx == 0) vs_launch<T, SUP, K>(in, out, H, W, s);
+  else if (dx == -1) ds_launch<T, SUP, K, 1>(in, out, H, W, s);
+  else ds_launch<T, SUP, K, -1>(in, out, H, W, s);
+}
+
 template <typename T, bool SUP>
-static bool vs_dispatch(const T *in, T *out, int H, int W, int k, cudaStream_t s) {
+static bool vs_dispatch(const T *in, T *out, int H, int W, int dx, int k, cudaStream_t s) {
   switch (k) {
-    case 1: vs_launch<T, SUP, 1>(in, out, H, W, s); return true;
-    case 2: vs_launch<T, SUP, 2>(in, out, H, W, s); return true;
-    case 3: vs_launch<T, SUP, 3>(in, out, H, W, s); return true;
-    case 7: vs_launch<T, SUP, 7>(in, out, H, W, s); return true;
-    case 15: vs_launch<T, SUP, 15>(in, out, H, W, s); return true;
-    case 31: vs_launch<T, SUP, 31>(in, out, H, W, s); return true;
+    case 1: line_launch<T, SUP, 1>(in, out, H, W, dx, s); return true;
+    case 2: line_launch<T, SUP, 2>(in, out, H, W, dx, s); return true;
+    case 3: line_launch<T, SUP, 3>(in, out, H, W, dx, s); return true;
+    case 7: line_launch<T, SUP, 7>(in, out, H, W, dx, s); return true;
+    case 15: line_launch<T, SUP, 15>(in, out, H, W, dx, s); return true;
+    case 31: line_launch<T, SUP, 31>(in, out, H, W, dx, s); return true;
     default: return false;
   }
 }
 
-// Fast path of launch_line for Y segments; false when the image or half length does not qualify.
+// Fast path of launch_line for Y and diagonal segments; false when the image or half length does
+// not qualify.
 bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
                      pg_status *st) {
   const int es = elem_size(in.ptype);
-  if (es > 4 || dx != 0 || dy != 1) return false;
+  if (es > 4 || dy != 1 || dx < -1 || dx > 1) return false;
+  // diagonals: 4-byte pixels only (for 1- and 2-byte pixels the word-packed staircase tiles of
+  // line_w.cu measured as fast or faster on 4096^2)
+  if (dx != 0 && es != 4) return false;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, W = d.nx;
-  if (H < 1 || H > (1 << 30) || W > (1 << 30) || ceil_div(H, 64) > 65535) return false;
-  if ((W * es) % 4 != 0) return false;
-  if ((reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 4 != 0) return false;
+  if (H < 1 || H > (1 << 30) || W > (1 << 29) || ceil_div(H, 32) > 65535) return false;
+  // the vertical kernel moves whole 32-bit words; the diagonal one single pixels
+  if (dx == 0 && (W * es) % 4 != 0) return false;
+  if (dx == 0 && (reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 4 != 0) return false;
   bool ok = false;
   switch (in.ptype) {
     case PG_PTYPE_U8: {
       using T = uint8_t;
-      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s)
-                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s);
+      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s)
+                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s);
       break;
     }
     case PG_PTYPE_U16: {
       using T = uint16_t;
-      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s)
-                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s);
+      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s)
+                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s);
       break;
     }
     case PG_PTYPE_I32: {
       using T = int32_t;
-      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s)
-                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s);
+      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s)
+                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s);
       break;
     }
     case PG_PTYPE_F32: {
       using T = float;
-      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s)
-                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, k, s);
+      ok = dilate ? vs_dispatch<T, true>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s)
+                  : vs_dispatch<T, false>((const T *)in.data, (T *)out.data, (int)H, (int)W, dx, k, s);
       break;
     }
     default: return false;

@@ -12,7 +12,9 @@
 //   * X:  E x E blocks are transposed while staging (__byte_perm), so columns become the scan
 //         positions and a word holds E adjacent rows; transposed back on output;
 //   * 45 / 135 degrees: staged row r is sheared by r pixels (funnel shifts), so the diagonal
-//         lines become columns.
+//         lines become columns.  The output tiles are staircases that lean along the diagonal
+//         (a tile row's word range moves by one word every E rows), so the sheared band a tile
+//         stages is only TX + 2E pixels wide, not TX + TY.
 // Per (word column, block of 2k+1 positions) one thread runs the running prefix into G and the
 // running suffix in place; out = op(suffix(p - k), prefix(p + k)).  Staging and output are
 // coalesced 32-bit accesses; shared rows have an odd word pitch (conflict-free scans).
@@ -34,6 +36,7 @@ struct LWGeom {
   int L;        // scan positions staged
   int NW, NWP;  // word lines and row pitch (odd)
   int nblk;     // blocks of 2k+1 positions per line
+  int txl;      // diagonals: staircase tiles left of tile 0 (blockIdx.x - txl is the tile column)
 };
 
 template <typename T, bool SUP, int MODE>
@@ -48,7 +51,8 @@ __global__ void __launch_bounds__(kLWThreads) k_line_w(const T *__restrict__ in,
   uint32_t *outw = reinterpret_cast<uint32_t *>(out);
   const T NEU = Op<T, SUP>::neutral();
   const uint32_t NEUW = splat<T>(NEU);
-  const int ty0 = blockIdx.y * g.TY, tx0 = blockIdx.x * g.TX;
+  const int ty0 = blockIdx.y * g.TY;
+  const int tx0 = (MODE == LW_D45 || MODE == LW_D135) ? ((int)blockIdx.x - g.txl) * g.TX : (int)blockIdx.x * g.TX;
   const int k = g.k;
 
   // ------------------------------------------------------------------ stage
@@ -93,7 +97,8 @@ __global__ void __launch_bounds__(kLWThreads) k_line_w(const T *__restrict__ in,
     for (int r = warp; r < g.L; r += NWARPS)
     for (int uw = lane; uw < g.NW; uw += 32) {
       const int gy = ty0 - k + r;
-      const int c0 = (MODE == LW_D45) ? tx0 + uw * E + k - r : tx0 + uw * E - (g.TY - 1) - k + r;
+      // staged pixel u of row r lies on diagonal u of the tile's band (x + y, resp. x - y, constant)
+      const int c0 = (MODE == LW_D45) ? tx0 + (g.TY - E) + uw * E + k - r : tx0 - (E - 1) + uw * E - k + r;
       uint32_t v = NEUW;
       if (gy >= 0 && gy < H && c0 + E > 0 && c0 < W) {
         if (c0 >= 0 && c0 + E <= W) {
@@ -174,13 +179,16 @@ __global__ void __launch_bounds__(kLWThreads) k_line_w(const T *__restrict__ in,
       }
     }
   } else {
+    // staircase row y: words [tx0 / E + sh, + XW) with sh = floor((TY - 1 - y) / E) (45 degrees) or
+    // floor(y / E) (135 degrees); its pixel e of word xw is diagonal E * xw + e + s of the band
     const int XW = g.TX / E;
     for (int y = warp; y < g.TY; y += NWARPS)
     for (int xw = lane; xw < XW; xw += 32) {
-      const int gy = ty0 + y, gw = tx0 / E + xw;
-      if (gy >= H || gw >= Wn) continue;
-      const int u = (MODE == LW_D45) ? xw * E + y : xw * E - y + g.TY - 1;
-      const int uw = u / E, s = u - uw * E;
+      const int m = (MODE == LW_D45) ? g.TY - 1 - y : y;
+      const int sh = m / E, s = E - 1 - (m - sh * E);
+      const int gy = ty0 + y, gw = tx0 / E + sh + xw;
+      if (gy >= H || gw < 0 || gw >= Wn) continue;
+      const int uw = xw;
       const uint32_t *f = F + y * g.NWP;
       const uint32_t *gg = G + (y + 2 * k) * g.NWP;
       const uint32_t a = shift_px<T>(f[uw], s ? f[uw + 1] : 0u, s);
@@ -202,9 +210,10 @@ static LWGeom lw_geom(int mode, int k, int TY, int TX) {
   g.TX = TX;
   if (mode == LW_V) { g.L = TY + 2 * k; g.NW = TX / E; }
   else if (mode == LW_H) { g.L = TX + 2 * g.KA; g.NW = TY / E; }
-  else { g.L = TY + 2 * k; g.NW = (TX + TY - 1) / E + 1; }
+  else { g.L = TY + 2 * k; g.NW = (TX + E - 1) / E + 1; }
   g.NWP = g.NW | 1;
   g.nblk = (g.L + 2 * k) / (2 * k + 1);  // ceil(L / (2k+1))
+  g.txl = 0;
   return g;
 }
 
@@ -223,18 +232,25 @@ static pg_status lw_launch(const T *in, T *out, int H, int W, int k, cudaStream_
       if (ok) break;
     }
   } else if (MODE == LW_H) {
-    for (int tx : {128, 64, 32}) {
-      for (int nw : {64, 32, 16, 8}) {
+    // wide, short tiles: measured best (4096^2, k = 15 and 31, u8/u16/f32) at 256 x 16 words
+    for (int tx : {256, 128, 64, 32}) {
+      for (int nw : {16, 32, 8, 64}) {
         g = lw_geom<T>(MODE, k, nw * E, tx);
         if (lw_smem(g) <= budget) { ok = true; break; }
       }
       if (ok) break;
     }
   } else {
-    for (int t : {64, 32, 16}) {
-      g = lw_geom<T>(MODE, k, t, t);
-      if (lw_smem(g) <= budget) { ok = true; break; }
+    // tall staircase tiles: the band staged per tile is (TY + 2k) x (TX + 2E) pixels
+    for (int ty : {128, 64, 32, 16}) {
+      for (int nw : {64, 32, 16}) {
+        g = lw_geom<T>(MODE, k, ty, nw * E);
+        if (lw_smem(g) <= budget) { ok = true; break; }
+      }
+      if (ok) break;
     }
+    const int shmax = (g.TY - 1) / E;  // largest staircase shift, in words
+    g.txl = (int)ceil_div(shmax, g.TX / E);
   }
   if (!ok && lw_smem(g) <= hard) ok = true;
   if (!ok) return fail(PG_ERR_INVALID_ARGUMENT, "segment too long for the word-packed line kernel");
@@ -247,7 +263,7 @@ static pg_status lw_launch(const T *in, T *out, int H, int W, int k, cudaStream_
                 "line kernel smem attribute");
     attr_devices.fetch_or(bit);
   }
-  dim3 grid((unsigned)ceil_div(W, g.TX), (unsigned)ceil_div(H, g.TY));
+  dim3 grid((unsigned)(ceil_div(W, g.TX) + g.txl), (unsigned)ceil_div(H, g.TY));
   if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the line kernel");
   k_line_w<T, SUP, MODE><<<grid, kLWThreads, lw_smem(g), s>>>(in, out, H, W, g);
   return cuda_status(cudaGetLastError(), "word-packed line kernel launch");
