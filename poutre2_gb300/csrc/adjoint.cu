@@ -217,115 +217,139 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_r(const float *__restri
 template <bool SUP, int R>
 __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restrict__ x, const float *__restrict__ gy,
                                                            float *__restrict__ gx, int H, int W) {
+  // Tile: AT_H x QW outputs, QW = 64 - 4R, so that the staged x band (QW + 4R) is exactly one
+  // column per thread of a 64-wide row and every phase is a single pass.
   constexpr int WX = 2 * R + 1;
   static_assert(WX * WX <= 32, "codes must fit a 32-bit mask");
-  constexpr int XH = AT_H + 4 * R, XW = AT_W + 4 * R;  // x over the tile + 2R
-  constexpr int PH = AT_H + 2 * R, PW = AT_W + 2 * R;  // outputs that can route into the tile
+  constexpr int QW = AF_TX - 4 * R;
+  constexpr int XH = AT_H + 4 * R, XW = AF_TX;         // x over the tile + 2R
+  constexpr int PH = AT_H + 2 * R, PW = QW + 2 * R;    // outputs that can route into the tile
+  constexpr int XR = (XH + AF_TY - 1) / AF_TY;         // staged x rows per thread
+  constexpr int PR = (PH + AF_TY - 1) / AF_TY;         // P rows per thread (contiguous)
   __shared__ float X[XH][XW + 1];
   __shared__ float RV[XH][PW + 1];
   __shared__ unsigned char RA[XH][PW + 1];
   __shared__ float G[PH][PW + 1];
-  __shared__ unsigned M[AT_H][AT_W];
+  __shared__ unsigned M[AT_H][QW];
+  __shared__ unsigned short HEAVY[AT_H * QW];  // tile pixels left to the second gather pass
+  __shared__ int n_heavy;
   const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
-  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * AT_W;
+  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * QW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *xp = x + plane;
   const float *gp = gy + plane;
-  // stage x (tile + 2R) and the upstream gradient (tile + R); clear the masks
-  {
-    constexpr int RI = (XH + AF_TY - 1) / AF_TY;
+  {  // stage x and the upstream gradient, loads first; clear the masks
+    const int xx = tx0 - 2 * R + tx;
+    const bool xin = xx >= 0 && xx < W;
+    float v[XR];
 #pragma unroll
-    for (int cc = 0; cc < XW; cc += AF_TX) {
-      const int c = cc + tx, xx = tx0 - 2 * R + c;
-      float v[RI];
-#pragma unroll
-      for (int k = 0; k < RI; ++k) {
-        const int r = tq + k * AF_TY, yy = ty0 - 2 * R + r;
-        const bool in = c < XW && r < XH && yy >= 0 && yy < H && xx >= 0 && xx < W;
-        v[k] = in ? __ldg(xp + (int64_t)yy * W + xx) : outside<SUP>();
-      }
-#pragma unroll
-      for (int k = 0; k < RI; ++k) {
-        const int r = tq + k * AF_TY;
-        if (c < XW && r < XH) X[r][c] = v[k];
-      }
+    for (int k = 0; k < XR; ++k) {
+      const int r = tq + k * AF_TY, yy = ty0 - 2 * R + r;
+      v[k] = (r < XH && xin && yy >= 0 && yy < H) ? __ldg(xp + (int64_t)yy * W + xx) : outside<SUP>();
     }
-    constexpr int RG = (PH + AF_TY - 1) / AF_TY;
+    const int gxx = tx0 - R + tx;
+    const bool gin = tx < PW && gxx >= 0 && gxx < W;
+    float g[PR];
 #pragma unroll
-    for (int cc = 0; cc < PW; cc += AF_TX) {
-      const int c = cc + tx, xx = tx0 - R + c;
-      float v[RG];
-#pragma unroll
-      for (int k = 0; k < RG; ++k) {
-        const int r = tq + k * AF_TY, yy = ty0 - R + r;
-        const bool in = c < PW && r < PH && yy >= 0 && yy < H && xx >= 0 && xx < W;
-        v[k] = in ? __ldg(gp + (int64_t)yy * W + xx) : 0.f;
-      }
-#pragma unroll
-      for (int k = 0; k < RG; ++k) {
-        const int r = tq + k * AF_TY;
-        if (c < PW && r < PH) G[r][c] = v[k];
-      }
+    for (int k = 0; k < PR; ++k) {
+      const int r = tq + k * AF_TY, yy = ty0 - R + r;
+      g[k] = (r < PH && gin && yy >= 0 && yy < H) ? __ldg(gp + (int64_t)yy * W + gxx) : 0.f;
     }
 #pragma unroll
-    for (int r = tq; r < AT_H; r += AF_TY) M[r][tx] = 0u;
+    for (int k = 0; k < XR; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < XH) X[r][tx] = v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < PR; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < PH && tx < PW) G[r][tx] = g[k];
+    }
+    if (tx < QW) {
+#pragma unroll
+      for (int r = tq; r < AT_H; r += AF_TY) M[r][tx] = 0u;
+    }
+    if (threadIdx.x == 0) n_heavy = 0;
   }
   __syncthreads();
   // row pass over the P columns: first strictly-best column of each row segment
-  for (int cc = 0; cc < PW; cc += AF_TX) {
-    const int c = cc + tx;
-    if (c < PW) {
-#pragma unroll 4
-      for (int r = tq; r < XH; r += AF_TY) {
-        float b = X[r][c];
+  if (tx < PW) {
+#pragma unroll
+    for (int k = 0; k < XR; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < XH) {
+        float b = X[r][tx];
         int a = 0;
 #pragma unroll
-        for (int d = 1; d <= 2 * R; ++d)
-          if (better<SUP>(X[r][c + d], b)) { b = X[r][c + d]; a = d; }
-        RV[r][c] = b;
-        RA[r][c] = (unsigned char)a;
+        for (int d = 1; d <= 2 * R; ++d) {
+          const float v = X[r][tx + d];
+          if (better<SUP>(v, b)) { b = v; a = d; }
+        }
+        RV[r][tx] = b;
+        RA[r][tx] = (unsigned char)a;
       }
     }
   }
   __syncthreads();
-  // column pass: each routing output's arg code, posted as a bit to the tile pixel it routes to
-  for (int cc = 0; cc < PW; cc += AF_TX) {
-    const int c = cc + tx;
-    if (c >= PW) continue;
-    const int xx = tx0 - R + c;
-#pragma unroll 2
-    for (int r = tq; r < PH; r += AF_TY) {
-      const int yy = ty0 - R + r;
-      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;  // not an output
-      float b = RV[r][c];
+  // column pass: each routing output's arg code, posted as a bit to the tile pixel it routes to.
+  // Thread (tx, tq) walks P rows [tq * PR, tq * PR + PR) of column tx with the window in registers.
+  if (tx < PW) {
+    const int xx = tx0 - R + tx;
+    const bool colin = xx >= 0 && xx < W;
+    const int r0 = tq * PR;
+    float col[PR + 2 * R];
+#pragma unroll
+    for (int i = 0; i < PR + 2 * R; ++i) col[i] = (r0 + i < XH) ? RV[r0 + i][tx] : outside<SUP>();
+#pragma unroll
+    for (int i = 0; i < PR; ++i) {
+      const int r = r0 + i, yy = ty0 - R + r;
+      if (r >= PH || !colin || yy < 0 || yy >= H) continue;  // not an output
+      float b = col[i];
       int a = 0;
 #pragma unroll
       for (int d = 1; d <= 2 * R; ++d)
-        if (better<SUP>(RV[r + d][c], b)) { b = RV[r + d][c]; a = d; }
-      const int ac = RA[r + a][c];
-      // the arg, in tile coordinates: output (r - R, c - R) + window (a - R, ac - R)
-      const int qr = r - 2 * R + a, qc = c - 2 * R + ac;
-      if (qr >= 0 && qr < AT_H && qc >= 0 && qc < AT_W) atomicOr(&M[qr][qc], 1u << (a * WX + ac));
+        if (better<SUP>(col[i + d], b)) { b = col[i + d]; a = d; }
+      const int ac = RA[r + a][tx];
+      // the arg in tile coordinates: output (r - R, tx - R) + window (a - R, ac - R)
+      const int qr = r - 2 * R + a, qc = tx - 2 * R + ac;
+      if (qr >= 0 && qr < AT_H && qc >= 0 && qc < QW) atomicOr(&M[qr][qc], 1u << (a * WX + ac));
     }
   }
   __syncthreads();
-  // gather: contributors in raster order = codes from high to low
-  float *op = gx + plane;
-  const int xx = tx0 + tx;
-#pragma unroll 2
-  for (int r = tq; r < AT_H; r += AF_TY) {
-    const int yy = ty0 + r;
-    if (yy >= H || xx >= W) continue;
-    unsigned m = M[r][tx];
+  // gather: contributors in raster order = codes from high to low.  Code c's contributor sits at
+  // G[r + 2R - c / WX][tx + 2R - c % WX].  A pixel with more than two contributors (a local
+  // extremum collects up to WX^2) goes to a list handled in a second pass, so that one lane's
+  // long chain does not hold up its warp.
+  auto gather = [&](int r, int c) -> float {
+    unsigned m = M[r][c];
+    const float *gq = &G[r + 2 * R][c + 2 * R];
     float sum = 0.f;
     while (m) {
       const int code = 31 - __clz(m);
-      m &= ~(1u << code);
-      const int a = code / WX, ac = code - a * WX;
-      // contributor p = q - (window offset) in P coordinates: (r + R) + R - a, (tx + R) + R - ac
-      sum += G[r + 2 * R - a][tx + 2 * R - ac];
+      m ^= 1u << code;
+      const int a = code / WX;
+      sum += gq[-(a * (PW + 1) + (code - a * WX))];
     }
-    op[(int64_t)yy * W + xx] = sum;
+    return sum;
+  };
+  float *op = gx + plane;
+  if (tx < QW) {
+    const int xx = tx0 + tx;
+#pragma unroll 4
+    for (int r = tq; r < AT_H; r += AF_TY) {
+      const int yy = ty0 + r;
+      if (yy >= H || xx >= W) continue;
+      if (__popc(M[r][tx]) > 2) {
+        HEAVY[atomicAdd(&n_heavy, 1)] = (unsigned short)(r * QW + tx);
+        continue;
+      }
+      op[(int64_t)yy * W + xx] = gather(r, tx);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_heavy; i += AT_THREADS) {
+    const int q = HEAVY[i], r = q / QW, c = q - r * QW;
+    op[(int64_t)(ty0 + r) * W + tx0 + c] = gather(r, c);
   }
 }
 
@@ -343,7 +367,7 @@ template <bool SUP>
 static bool flat_bwd_fixed(const float *x, const float *g, float *o, int64_t planes, int64_t h, int64_t w, int ry, int rx,
                            cudaStream_t s) {
   if (ry != rx || ry < 1 || ry > 2 || planes > 65535) return false;  // (2R+1)^2 <= 32
-  const dim3 grid((unsigned)ceil_div(w, AT_W), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
+  const dim3 grid((unsigned)ceil_div(w, AF_TX - 4 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
   if (ry == 1) k_flat_bwd_r<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
   else k_flat_bwd_r<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
   return true;

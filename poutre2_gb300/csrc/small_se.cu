@@ -160,15 +160,38 @@ __global__ void __launch_bounds__(256) k_small3d(const T *__restrict__ in, T *__
   auto slice = [&](int64_t z, P &A, P &B) {
     if (z < 0 || z >= D) { A = P::fill(NEU); B = A; return; }
     const T *rm = row_m + z * plane;
+    if constexpr (SHAPE == SH_SQUARE) {
+      // separable: the column max of the three rows first (and of their edge neighbours), then
+      // one horizontal 3-neighbourhood instead of three
+      const T *ru = rm - W, *rd = rm + W;
+      const P cu = has_up ? P::load(ru + x0) : P::fill(NEU);
+      const P cm = P::load(rm + x0);
+      const P cd = has_dn ? P::load(rd + x0) : P::fill(NEU);
+      T left = NEU, right = NEU;
+      if (x0 > 0) {
+        left = ldg(rm + x0 - 1);
+        if (has_up) left = Op<T, SUP>::apply(left, ldg(ru + x0 - 1));
+        if (has_dn) left = Op<T, SUP>::apply(left, ldg(rd + x0 - 1));
+      }
+      if (x0 + P::N < W) {
+        right = ldg(rm + x0 + P::N);
+        if (has_up) right = Op<T, SUP>::apply(right, ldg(ru + x0 + P::N));
+        if (has_dn) right = Op<T, SUP>::apply(right, ldg(rd + x0 + P::N));
+      }
+      const P v = P::template op<SUP>(P::template op<SUP>(cu, cm), cd);
+      A = P::template op<SUP>(P::template op<SUP>(v, v.shl(left)), v.shr(right));
+      B = A;
+      return;
+    }
     P cu, hu, cm, hm, cd, hd;
-    const bool need_rows = (SHAPE == SH_SQUARE || SHAPE == SH_CROSS || SHAPE == SH_SEGY);
+    const bool need_rows = (SHAPE == SH_CROSS || SHAPE == SH_SEGY);
     const bool need_h = (SHAPE != SH_SEGY && SHAPE != SH_SEGZ);
     load_row<T, SUP>(rm, true, x0, W, need_h, cm, hm);
     if (need_rows) {
-      load_row<T, SUP>(rm - W, has_up, x0, W, SHAPE == SH_SQUARE, cu, hu);
-      load_row<T, SUP>(rm + W, has_dn, x0, W, SHAPE == SH_SQUARE, cd, hd);
+      load_row<T, SUP>(rm - W, has_up, x0, W, false, cu, hu);
+      load_row<T, SUP>(rm + W, has_dn, x0, W, false, cd, hd);
     }
-    if constexpr (SHAPE == SH_SQUARE) { A = P::template op<SUP>(P::template op<SUP>(hu, hm), hd); B = A; }
+    if constexpr (SHAPE == SH_SQUARE) { A = P::fill(NEU); B = A; }
     else if constexpr (SHAPE == SH_CROSS) { A = P::template op<SUP>(P::template op<SUP>(cu, hm), cd); B = cm; }
     else if constexpr (SHAPE == SH_SEGX) { A = hm; B = P::fill(NEU); }
     else if constexpr (SHAPE == SH_SEGY) { A = P::template op<SUP>(P::template op<SUP>(cu, cm), cd); B = P::fill(NEU); }
