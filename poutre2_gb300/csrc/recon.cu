@@ -545,6 +545,14 @@ template <typename T> __device__ __forceinline__ T shfl_dn1(T v) {
   else return __shfl_down_sync(0xffffffffu, v, 1);
 }
 
+// element e (a compile-time constant after unrolling) of a 16-byte vector of 1- or 2-byte pixels
+template <typename T> __device__ __forceinline__ T vec_elem(const uint4 &v, int e) {
+  constexpr int PW = 4 / (int)sizeof(T);  // pixels per 32-bit word
+  const int w = e / PW, sh = (e % PW) * 8 * (int)sizeof(T);
+  const uint32_t word = w == 0 ? v.x : w == 1 ? v.y : w == 2 ? v.z : v.w;
+  return (T)(word >> sh);
+}
+
 // One visit of a register tile: stage it from the reconstruction buffer (which the worklist
 // kernel's first phase set to the marker), iterate sweep sets to the tile-local fixpoint (or
 // P.max_sweeps), write it back if anything changed.  Returns the B_* bits of the borders that
@@ -580,11 +588,48 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
   }
 
   // stage, lane = column: tile values and mask (pixels outside the image: neutral, fixed).
-  // Loads come first, 16 rows at a time, so that they are all in flight together.
   const T *mk_in = static_cast<const T *>(im.marker);
   const T *ms_in = static_cast<const T *>(im.mask);
   const bool need_mk = needs_marker(P, 1);
   T v[32];
+  bool vec = false;
+  if constexpr (sizeof(T) <= 2) {
+    // rows of whole 16-byte vectors: the tile (32 rows x 32 or 64 bytes) comes in 2 * sizeof(T)
+    // vector loads per lane and array, unpacked into shared memory; v is then read per column
+    vec = (im.W * (int64_t)sizeof(T)) % 16 == 0 &&
+          ((reinterpret_cast<uintptr_t>(ms_in) | reinterpret_cast<uintptr_t>(rec_in) |
+            (need_mk ? reinterpret_cast<uintptr_t>(mk_in) : (uintptr_t)0)) % 16) == 0;
+  }
+  if (vec) {
+    constexpr int VPR = 2 * (int)sizeof(T);   // 16-byte vectors per tile row
+    constexpr int VPX = 16 / (int)sizeof(T);  // pixels per vector
+    uint4 ma[VPR], ka[VPR], ra[VPR];
+#pragma unroll
+    for (int k = 0; k < VPR; ++k) {
+      const int q = k * 32 + lane, row = q / VPR, vc = q % VPR;
+      const int64_t gy = y0 + row, gx0 = x0 + vc * VPX;
+      const int64_t gi = (gy < im.H && gx0 < im.W) ? gy * im.W + gx0 : 0;
+      ma[k] = __ldg(reinterpret_cast<const uint4 *>(ms_in + gi));
+      ka[k] = need_mk ? __ldg(reinterpret_cast<const uint4 *>(mk_in + gi)) : ma[k];
+      ra[k] = __ldcg(reinterpret_cast<const uint4 *>(rec_in + gi));
+    }
+#pragma unroll
+    for (int k = 0; k < VPR; ++k) {
+      const int q = k * 32 + lane, row = q / VPR, vc = q % VPR;
+      const bool ok = y0 + row < im.H && x0 + vc * VPX < im.W;
+#pragma unroll
+      for (int e = 0; e < VPX; ++e) {
+        const T a = vec_elem<T>(ma[k], e), b = vec_elem<T>(ka[k], e), c = vec_elem<T>(ra[k], e);
+        s_m[row * kRP + vc * VPX + e] = ok ? combine_mask(P, a, b) : NEU;
+        s_t[row * kRP + vc * VPX + e] = ok ? c : NEU;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; ++r) v[r] = (T)s_t[r * kRP + lane];
+    __syncwarp();
+  } else {
+  // scalar stage: loads come first, 16 rows at a time, so that they are all in flight together
 #pragma unroll
   for (int h = 0; h < 32; h += 16) {
     T a[16], b[16];
@@ -606,6 +651,7 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
       }
       s_m[(h + r) * kRP + lane] = m;
     }
+  }
   }
   T top = hv[0], bot = hv[1], hl = hv[2], hr = hv[3];
   if (CONN8) {
