@@ -553,6 +553,143 @@ template <typename T> __device__ __forceinline__ T vec_elem(const uint4 &v, int 
   return (T)(word >> sh);
 }
 
+// Sweep sets of a 32x32 tile of 1- or 2-byte pixels with two rows per 32-bit register: pair p
+// holds row p (low half) and row 31 - p (high half) of the lane's column, so the two chains that
+// the vertical sweeps run at once (down over the top half with up over the bottom half, then the
+// reverse) advance together in one 2x16-bit min/max per step; after the transpose, pair c holds
+// columns c and 31 - c of the lane's row and the horizontal chains pair up the same way.  The
+// masks are packed the same way.  Same updates, in the same order, as the
+// unpacked sweeps.  Returns through v (unpacked) and the flags; s_m is overwritten.
+__device__ __forceinline__ uint32_t u16x2_max(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("max.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t u16x2_min(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm("min.u16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t pk2(uint32_t lo, uint32_t hi) { return (lo & 0xffffu) | (hi << 16); }
+__device__ __forceinline__ uint32_t swap2(uint32_t x) { return __byte_perm(x, 0, 0x1032); }
+
+__device__ __forceinline__ uint32_t lds_u32(const uint32_t *p) {  // see lds_mask
+  const unsigned addr = (unsigned)__cvta_generic_to_shared(p);
+  uint32_t r;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(r) : "r"(addr));
+  return r;
+}
+
+template <typename T, bool SUP, bool CONN8>
+__device__ void sweeps_packed(T (&v)[32], RegS<T> *s_m, RegS<T> *s_t, int max_sweeps, T top, T bot, T hl, T hr,
+                              T initL, T initR, bool &converged, bool &changed, bool &wch, bool &ech) {
+  static_assert(sizeof(T) <= 2, "two pixels per register");
+  const int lane = threadIdx.x & 31;
+  auto OS = [](uint32_t a, uint32_t b) { return SUP ? u16x2_max(a, b) : u16x2_min(a, b); };  // propagation
+  auto OC = [](uint32_t a, uint32_t b) { return SUP ? u16x2_min(a, b) : u16x2_max(a, b); };  // clip by the mask
+  // packed masks, rewritten over the unpacked ones: rows 0-15 of s_m hold the column pairs
+  // (lane = column), rows 16-31 the row pairs (lane = row)
+  uint32_t P[16];
+  {
+    uint32_t MA[16], MB[16];
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+      MA[p] = pk2((uint32_t)s_m[p * kRP + lane], (uint32_t)s_m[(31 - p) * kRP + lane]);
+      MB[p] = pk2((uint32_t)s_m[lane * kRP + p], (uint32_t)s_m[lane * kRP + 31 - p]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+      s_m[p * kRP + lane] = MA[p];
+      s_m[(16 + p) * kRP + lane] = MB[p];
+    }
+    __syncwarp();
+  }
+  const uint32_t *MAs = reinterpret_cast<const uint32_t *>(s_m) + lane;
+  const uint32_t *MBs = reinterpret_cast<const uint32_t *>(s_m) + 16 * kRP + lane;
+#pragma unroll
+  for (int p = 0; p < 16; ++p) P[p] = pk2(v[p], v[31 - p]);
+  const uint32_t tb = pk2(top, bot), lr = pk2(hl, hr);
+  auto nbrow = [&](uint32_t x) -> uint32_t {
+    if (CONN8) {
+      const uint32_t a = __shfl_up_sync(0xffffffffu, x, 1), b = __shfl_down_sync(0xffffffffu, x, 1);
+      return OS(x, OS(a, b));
+    }
+    return x;
+  };
+  converged = false;
+  changed = false;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    uint32_t ch = 0;
+    // vertical: pair k from pair k - 1 (k = 0: the halo rows), then pair 15 from itself swapped
+    // and pair q from pair q + 1
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t nb = k == 0 ? tb : nbrow(P[k - 1]);  // the halo rows are already 3-wide
+      const uint32_t nv = OC(OS(P[k], nb), lds_u32(MAs + k * kRP));
+      ch |= nv ^ P[k];
+      P[k] = nv;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int q = 15 - k;
+      const uint32_t nb = nbrow(k == 0 ? swap2(P[15]) : P[q + 1]);
+      const uint32_t nv = OC(OS(P[q], nb), lds_u32(MAs + q * kRP));
+      ch |= nv ^ P[q];
+      P[q] = nv;
+    }
+    // to lane = row
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+      s_t[p * kRP + lane] = P[p] & 0xffffu;
+      s_t[(31 - p) * kRP + lane] = P[p] >> 16;
+    }
+    __syncwarp();
+    uint32_t Q[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) Q[c] = pk2((uint32_t)s_t[lane * kRP + c], (uint32_t)s_t[lane * kRP + 31 - c]);
+    __syncwarp();
+    // horizontal, the same pairing
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t nb = k == 0 ? lr : Q[k - 1];
+      const uint32_t nv = OC(OS(Q[k], nb), lds_u32(MBs + k * kRP));
+      ch |= nv ^ Q[k];
+      Q[k] = nv;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int q = 15 - k;
+      const uint32_t nb = k == 0 ? swap2(Q[15]) : Q[q + 1];
+      const uint32_t nv = OC(OS(Q[q], nb), lds_u32(MBs + q * kRP));
+      ch |= nv ^ Q[q];
+      Q[q] = nv;
+    }
+    wch = (T)(Q[0] & 0xffffu) != initL;
+    ech = (T)(Q[0] >> 16) != initR;
+    // back to lane = column
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      s_t[lane * kRP + c] = Q[c] & 0xffffu;
+      s_t[lane * kRP + 31 - c] = Q[c] >> 16;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < 16; ++p) P[p] = pk2((uint32_t)s_t[p * kRP + lane], (uint32_t)s_t[(31 - p) * kRP + lane]);
+    __syncwarp();
+    if (!__any_sync(0xffffffffu, ch != 0)) {
+      converged = true;
+      break;
+    }
+    changed = true;
+  }
+#pragma unroll
+  for (int p = 0; p < 16; ++p) {
+    v[p] = (T)(P[p] & 0xffffu);
+    v[31 - p] = (T)(P[p] >> 16);
+  }
+}
+
 // One visit of a register tile: stage it from the reconstruction buffer (which the worklist
 // kernel's first phase set to the marker), iterate sweep sets to the tile-local fixpoint (or
 // P.max_sweeps), write it back if anything changed.  Returns the B_* bits of the borders that
@@ -669,6 +806,9 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
   __syncwarp();
 
   bool converged = false, changed = false, wch = false, ech = false;
+  if constexpr (sizeof(T) <= 2) {
+    sweeps_packed<T, SUP, CONN8>(v, s_m, s_t, P.max_sweeps, top, bot, hl, hr, initL, initR, converged, changed, wch, ech);
+  } else {
   for (int sweep = 0; sweep < P.max_sweeps; ++sweep) {
     bool ch = false;
     auto vstep = [&](int r, T nb) {
@@ -739,6 +879,7 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
     changed = true;
   }
 
+  }
   const unsigned bN = __ballot_sync(0xffffffffu, v[0] != initT);
   const unsigned bS = __ballot_sync(0xffffffffu, v[31] != initB);
   const unsigned bW = __ballot_sync(0xffffffffu, wch);
