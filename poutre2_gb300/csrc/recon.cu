@@ -894,7 +894,31 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
   if (bS & 1u) f |= B_SW;
   if (bS >> 31) f |= B_SE;
 
-  if (changed) {
+  if (changed && vec) {
+    // the stage's vector layout in reverse: columns to shared memory, rows out as 16-byte stores
+    if constexpr (sizeof(T) <= 2) {
+      constexpr int VPR = 2 * (int)sizeof(T), VPX = 16 / (int)sizeof(T), PW = 4 / (int)sizeof(T);
+#pragma unroll
+      for (int r = 0; r < 32; ++r) s_t[r * kRP + lane] = v[r];
+      __syncwarp();
+      T *rec = static_cast<T *>(im.rec);
+#pragma unroll
+      for (int k = 0; k < VPR; ++k) {
+        const int q = k * 32 + lane, row = q / VPR, vc = q % VPR;
+        const int64_t gy = y0 + row, gx0 = x0 + vc * VPX;
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          w[j] = 0u;
+#pragma unroll
+          for (int e = 0; e < PW; ++e)
+            w[j] |= ((uint32_t)s_t[row * kRP + vc * VPX + j * PW + e] & Lim<T>::hi()) << (8 * (int)sizeof(T) * e);
+        }
+        if (gy < im.H && gx0 < im.W) __stcg(reinterpret_cast<uint4 *>(rec + gy * im.W + gx0), make_uint4(w[0], w[1], w[2], w[3]));
+      }
+      __syncwarp();
+    }
+  } else if (changed) {
     // the row stride goes through a shuffle so that the compiler recomputes these addresses
     // here instead of keeping the stage's 32 row addresses alive across the sweeps
     const long long Wd = __shfl_sync(0xffffffffu, (long long)im.W, 0);
