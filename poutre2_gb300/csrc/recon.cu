@@ -946,12 +946,18 @@ __device__ int process_tile_reg(const RImg &im, const RParams<T> &P, int t_local
 // field 0).  No compare-and-swap retries on the shared counters.
 enum : unsigned { TS_IDLE = 0, TS_QUEUED = 1, TS_RUNNING = 2, TS_DIRTY = 3 };
 
-struct RQueue {             // each counter on its own 128-byte line
-  unsigned head, pad0[31];  // next ticket to pop
-  unsigned tail, pad1[31];  // next position to push
-  int pending, pad2[31];    // tiles queued or being visited
-  unsigned pad3[32];
+// `tail` (next position to push, low 32 bits) and `pending` (tiles queued or being visited, high
+// 32 bits) share one 64-bit word, so that a warp counts the tiles it pushes and reserves their
+// positions in one atomic: a tile cannot be popped and finished (pending - 1) before its own
+// pending + 1 is performed.
+struct RQueue {                // each counter on its own 128-byte line
+  unsigned head, pad0[31];     // next ticket to pop
+  unsigned long long tp;       // pending << 32 | tail
+  unsigned pad1[30];
+  unsigned pad2[64];
 };
+__device__ __forceinline__ unsigned tp_tail(unsigned long long tp) { return (unsigned)tp; }
+__device__ __forceinline__ int tp_pending(unsigned long long tp) { return (int)(tp >> 32); }
 static_assert(sizeof(RQueue) == 512, "RQueue layout");
 
 template <typename T> struct WorkList {
@@ -988,7 +994,7 @@ __device__ int wl_pop(const WorkList<T> &wl, RCtl *ctl, long long max_tickets) {
   for (;;) {
     v = *slot;
     if ((unsigned)(v >> 32) == pos && (unsigned)v != 0u) break;
-    if (*((volatile int *)&wl.q->pending) == 0) return -1;
+    if (tp_pending(*((volatile unsigned long long *)&wl.q->tp)) == 0) return -1;
     if (*((volatile int *)&ctl->status) != 0) return -1;
     __nanosleep(ns);
     if (ns < 4096) ns <<= 1;
@@ -1053,8 +1059,7 @@ __device__ void wl_finish(const WorkList<T> &wl, RCtl *ctl, const RImg &im, int 
   const int n = __popc(pm);
   unsigned base = 0;
   if (lane == 0 && n > 0) {
-    atomicAdd(&wl.q->pending, n);
-    base = atomicAdd(&wl.q->tail, (unsigned)n);
+    base = tp_tail(atomicAdd(&wl.q->tp, ((unsigned long long)n << 32) | (unsigned long long)n));
   }
   base = __shfl_sync(0xffffffffu, base, 0);
   if (push) {
@@ -1068,7 +1073,8 @@ __device__ void wl_finish(const WorkList<T> &wl, RCtl *ctl, const RImg &im, int 
     }
     *slot = slot_val(pos, (unsigned)cand + 1u);
   }
-  if (lane == 0) atomicSub(&wl.q->pending, 1);  // after this warp's pushes were counted: never 0 early
+  // pending - 1, after this warp's pushes were counted (same word, same thread): never 0 early
+  if (lane == 0) atomicAdd(&wl.q->tp, ~0ull << 32);
 }
 
 // first phase: every reconstruction buffer starts at the marker (select_marker, or the
@@ -1121,8 +1127,7 @@ __global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T>
     if (i < P.ntiles) wl.state[i] = TS_QUEUED;
   }
   if (tid == 0) {
-    wl.q->tail = (unsigned)P.ntiles;
-    wl.q->pending = P.ntiles;
+    wl.q->tp = ((unsigned long long)P.ntiles << 32) | (unsigned long long)P.ntiles;
   }
   if (!grid_barrier(ctl)) return;
 
@@ -1145,7 +1150,7 @@ __global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T>
   }
   if (!grid_barrier(ctl)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    const long long visits = (long long)*((volatile unsigned *)&wl.q->tail);  // every pushed tile was visited
+    const long long visits = (long long)tp_tail(*((volatile unsigned long long *)&wl.q->tp));  // every pushed tile was visited
     g_recon_visits = visits;
     g_recon_rounds = (int)((visits + P.ntiles - 1) / P.ntiles);
     ctl->rounds = g_recon_rounds;
