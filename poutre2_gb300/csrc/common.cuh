@@ -97,46 +97,6 @@ template <typename T> struct Pack {
   }
 };
 
-// Two adjacent packs (32 bytes): twice the bytes in flight per thread, same interface.
-template <typename T> struct Pack2 {
-  static constexpr int N = 2 * Pack<T>::N;
-  Pack<T> a, b;
-  __device__ __forceinline__ static Pack2 load(const T *p) {
-    Pack2 r;
-    r.a = Pack<T>::load(p);
-    r.b = Pack<T>::load(p + Pack<T>::N);
-    return r;
-  }
-  __device__ __forceinline__ void store(T *p) const {
-    a.store(p);
-    b.store(p + Pack<T>::N);
-  }
-  __device__ __forceinline__ static Pack2 fill(T x) {
-    Pack2 r;
-    r.a = Pack<T>::fill(x);
-    r.b = r.a;
-    return r;
-  }
-  template <bool SUP> __device__ __forceinline__ static Pack2 op(const Pack2 &x, const Pack2 &y) {
-    Pack2 r;
-    r.a = Pack<T>::template op<SUP>(x.a, y.a);
-    r.b = Pack<T>::template op<SUP>(x.b, y.b);
-    return r;
-  }
-  __device__ __forceinline__ Pack2 shl(T left) const {
-    Pack2 r;
-    r.a = a.shl(left);
-    r.b = b.shl(a.last());
-    return r;
-  }
-  __device__ __forceinline__ Pack2 shr(T right) const {
-    Pack2 r;
-    r.a = a.shr(b.first());
-    r.b = b.shr(right);
-    return r;
-  }
-};
-
 // ------------------------------------------------------------------ host-side plumbing
 void set_error(const std::string &msg);
 pg_status fail(pg_status st, const std::string &msg);

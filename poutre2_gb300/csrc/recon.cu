@@ -9,22 +9,24 @@
 // scheme below is bit-exact with it.  Leveling (leveling_t.hpp:45-202) is the same fixpoint
 // with mask max(marker, ref) (low) / min(marker, ref) (high) followed by a clip by ref.
 //
-// GPU design
-//  * The image is cut into 64x64 tiles.  A CTA (64 threads) stages a tile of the current
-//    reconstruction plus a one-pixel halo, and the tile's mask, in shared memory and iterates
-//    directional sweeps there -- down, up (thread per column), right, left (thread per row),
-//    each propagating along its whole direction in one pass -- until a full sweep set
-//    changes nothing: a tile-local fixpoint.  It writes the tile back and flags the
-//    neighbouring tiles whose shared border changed.
-//  * A persistent cooperative grid (all CTAs resident) runs rounds over the flagged tiles
-//    (round 0: all tiles, marker computed from the inputs), separated by a grid barrier,
-//    until a round flags nothing.  Flags live in a double-buffered device worklist; the
-//    "any flag" word is triple-buffered so no CTA resets a word another may still read.
+// GPU design: tiles iterated to a tile-local fixpoint, scheduled until no tile changes.
+//  * Pixels of at most 4 bytes (k_reconstruct_wl): 32x32 tiles, one warp per tile, the tile
+//    in registers; directional sweep sets (down/up by warp shuffles, right/left after a
+//    shared-memory transpose; two rows per register for 1- and 2-byte pixels) until a set
+//    changes nothing.  The tiles are driven by a device worklist (a ticket ring and a state
+//    per tile, below): a warp pops a tile, visits it, and queues the neighbours whose shared
+//    border changed, until no tile is queued or running.
+//  * 8-byte pixels, the allocation-free entry and one batch-plan configuration
+//    (k_reconstruct): 64x64 (32x32) tiles staged in shared memory with a one-pixel halo and
+//    swept by a CTA; rounds over the flagged tiles (round 0: all tiles, marker computed from
+//    the inputs) separated by a grid barrier, until a round flags nothing.  Flags live in a
+//    double-buffered device worklist; the "any flag" word is triple-buffered so no CTA resets
+//    a word another may still read.
 //  * Reads of other tiles' pixels bypass L1 (ld.global.cg): values only grow (shrink for
 //    erosion), so a concurrently updated halo value is either the old or the new one, both
-//    below the fixpoint; a tile that saw an old value is re-flagged by its writer.
-//  * Every wait is bounded: the grid barrier gives up after kBarrierTimeoutNs and the round
-//    loop after max_rounds, recording PG_ERR_NOT_CONVERGED in a device status word.
+//    below the fixpoint; a tile that saw an old value is queued (flagged) again by its writer.
+//  * Every wait is bounded (kBarrierTimeoutNs of %globaltimer on the grid barrier and on the
+//    worklist; visit and round caps), recording PG_ERR_NOT_CONVERGED in a device status word.
 #include <algorithm>
 #include <atomic>
 #include <cmath>

@@ -239,7 +239,6 @@ static int rows_per_thread(int64_t threads_without_strips, int64_t length, int c
 template <typename T, bool SUP, int SHAPE>
 static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream_t s) {
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
-  const bool vec2 = false;  // two packs per thread measured slower than one
   const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
   const int R = rows_per_thread(npack, H, 32);
@@ -247,8 +246,7 @@ static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream
   dim3 block(bx, 256 / bx);
   dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(ceil_div(H, R), 256 / bx));
   if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the small-SE kernel");
-  if (vec2) k_small2d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
-  else if (vec) k_small2d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
+  if (vec) k_small2d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   else k_small2d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 2D kernel launch");
 }
@@ -256,7 +254,6 @@ static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream
 template <typename T, bool SUP, int SHAPE>
 static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W, cudaStream_t s) {
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
-  const bool vec2 = false;  // two packs per thread measured slower than one
   const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
   const int R = rows_per_thread(npack * H, D, 16);
@@ -265,8 +262,7 @@ static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W,
   dim3 block(bx, 256 / bx);
   dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(H, 256 / bx), (unsigned)ceil_div(D, R));
   if (grid.y > 65535 || grid.z > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "volume too large for the small-SE kernel");
-  if (vec2) k_small3d<T, SUP, SHAPE, Pack2<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
-  else if (vec) k_small3d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
+  if (vec) k_small3d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   else k_small3d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, D, H, W, npack, R);
   return cuda_status(cudaGetLastError(), "small-SE 3D kernel launch");
 }
