@@ -109,6 +109,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(t_local, ws, device):
+    """The slowest rank's step time (the job's time); the identity on one process."""
+    if ws <= 1:
+        return t_local
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t_local)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_value(pixels_per_rank, ws, t_step):
+    """Whole-job throughput of `ws` replicas, each processing `pixels_per_rank` per step, in Gpixel/s."""
+    return ws * pixels_per_rank / t_step / 1e9
+
+
 def workload_image(size):
     from poutre2_gb300 import synthetic
     return synthetic.smoothed_noise_u8((size, size), seed=1, sigma=4.0)
@@ -379,13 +395,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
     clocks = clk.summary()
     ms = [a.elapsed_time(b) for a, b in ev]
-    t_step = sum(ms) / len(ms) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(sum(ms) / len(ms) / 1e3, ws, dev)
     _lib.call("pg_check_device", None)
-    value = ws * N / t_step / 1e9
+    value = replica_value(N, ws, t_step)
 
     # parity of the timed output against the oracle (outside the timed region)
     import oracle
@@ -407,11 +419,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_ms.append(a.elapsed_time(b))
-    t_e2e = sum(e2e_ms) / len(e2e_ms) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(sum(e2e_ms) / len(e2e_ms) / 1e3, ws, dev)
 
     peak, peak_kind = peaks()
     alg_bytes = 2 * N  # mask read + binary output written, per launch
@@ -425,7 +433,7 @@ def run_gpu(args):
                    "l2": "flushed between timed steps (256 MB read, untimed)", "rounds": rounds,
                    "parallelism": f"replicas x{ws}"},
         "parity_vs_oracle": parity,
-        "e2e": {"value": ws * N / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(N), "d2h_bytes_per_step": int(N)},
+        "e2e": {"value": replica_value(N, ws, t_e2e), "unit": UNIT, "h2d_bytes_per_step": int(N), "d2h_bytes_per_step": int(N)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_for(f"k_reconstruct_wl@hmaxima{args.size}"),
                      "peak_source": f"{peak_kind} hbm_gbs (burst)", "kernel": "k_reconstruct_wl<u8,dilate,8-conn>",
