@@ -494,3 +494,32 @@ def test_errors_mirror_reference_checks():
         geo.Reconstruction(geo.reconstruction_type.dilate, x, x.clone(), Common_NL_SE.SESegmentX2D, torch.empty_like(x))
     with pytest.raises(PoutreError):
         llm.Dilate(x.cpu(), Common_NL_SE.SESquare2D, 1, torch.empty_like(x))
+
+
+# ----------------------------------------------------------------------------- empty images
+@pytest.mark.parametrize("shape", [(0, 0), (0, 7), (5, 0)])
+def test_empty_images_are_accepted(shape):
+    # poutre2 images may have a zero extent; every entry point returns without computing
+    from poutre2_gb300 import geo, llm
+    from poutre2_gb300.se import Common_NL_SE
+    x = torch.zeros(shape, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(shape, dtype=torch.uint8, device="cuda")
+    for se in ("SESquare2D", "SECross2D", "SESegmentX2D", "SESegmentY2D"):
+        llm.Dilate(x, Common_NL_SE[se], 2, out)
+        llm.Erode(x, Common_NL_SE[se], 1, out)
+    llm.DilateX(x, 3, out)
+    llm.ErodeSE(x, llm.se_rect(2, 3), out)
+    llm.DilateSE(x, llm.se_line(-1, 1, 4), out)
+    llm.Opening(x, llm.se_rect(1, 1), out)
+    llm.Gradient(x, llm.se_static(Common_NL_SE.SESquare2D, 1), out)
+    if shape[0] == shape[1]:
+        llm.DilateY(x, 2, out)
+    geo.Reconstruction(geo.reconstruction_type.dilate, x, x.clone(), Common_NL_SE.SESquare2D, out)
+    geo.h_maxima(x, 3, Common_NL_SE.SESquare2D, out)
+    geo.h_maxima_binary(x, 3, Common_NL_SE.SESquare2D, out)
+    geo.leveling(x, x.clone(), Common_NL_SE.SECross2D, out)
+    y = torch.zeros((3, 4), dtype=torch.uint8, device="cuda")
+    oy = torch.empty_like(y)
+    geo.h_maxima_binary_batch([x, y], 3, Common_NL_SE.SESquare2D, [out, oy])
+    np.testing.assert_array_equal(host(oy), oracle.h_maxima_binary(np.zeros((3, 4), np.uint8), 3, "SESquare2D"))
+    torch.cuda.synchronize()
