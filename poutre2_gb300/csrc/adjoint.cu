@@ -161,56 +161,61 @@ template <bool SUP> __device__ __forceinline__ float best_of(float a, float b) {
 
 template <bool SUP, int R>
 __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_r(const float *__restrict__ x, float *__restrict__ y, int H, int W) {
-  constexpr int XH = AT_H + 2 * R, XW = AT_W + 2 * R;
+  // Tile: AT_H x FW outputs, FW = 64 - 2R, so that the staged band (FW + 2R) is exactly one
+  // column per thread of a 64-wide row and every phase is a single pass.
+  constexpr int FW = AF_TX - 2 * R;
+  constexpr int XH = AT_H + 2 * R, XW = AF_TX;
   __shared__ float X[XH][XW + 1];
-  __shared__ float RV[XH][AT_W + 1];
+  __shared__ float RV[XH][FW + 1];
   const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
-  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * AT_W;
+  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * FW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *xp = x + plane;
   constexpr int RI = (XH + AF_TY - 1) / AF_TY;  // staged rows per thread
-#pragma unroll
-  for (int cc = 0; cc < XW; cc += AF_TX) {
-    const int c = cc + tx;
-    const int gx = tx0 - R + c;
+  {
+    const int gx = tx0 - R + tx;
+    const bool colin = gx >= 0 && gx < W;
     float v[RI];
 #pragma unroll
     for (int k = 0; k < RI; ++k) {
       const int r = tq + k * AF_TY, gy = ty0 - R + r;
-      const bool in = c < XW && r < XH && gy >= 0 && gy < H && gx >= 0 && gx < W;
-      v[k] = in ? __ldg(xp + (int64_t)gy * W + gx) : outside<SUP>();
+      v[k] = (r < XH && colin && gy >= 0 && gy < H) ? __ldg(xp + (int64_t)gy * W + gx) : outside<SUP>();
     }
 #pragma unroll
     for (int k = 0; k < RI; ++k) {
       const int r = tq + k * AF_TY;
-      if (c < XW && r < XH) X[r][c] = v[k];
+      if (r < XH) X[r][tx] = v[k];
     }
   }
   __syncthreads();
+  if (tx < FW) {
 #pragma unroll
-  for (int k = 0; k < RI; ++k) {
-    const int r = tq + k * AF_TY;
-    if (r < XH) {
-      float b = X[r][tx];
+    for (int k = 0; k < RI; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < XH) {
+        float b = X[r][tx];
 #pragma unroll
-      for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, X[r][tx + d]);
-      RV[r][tx] = b;
+        for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, X[r][tx + d]);
+        RV[r][tx] = b;
+      }
     }
   }
   __syncthreads();
-  float *yp = y + plane;
-  constexpr int OR = AT_H / AF_TY;  // output rows per thread, consecutive
-  const int r0 = tq * OR, gx = tx0 + tx;
-  float col[OR + 2 * R];
+  if (tx < FW) {
+    float *yp = y + plane;
+    constexpr int OR = AT_H / AF_TY;  // output rows per thread, consecutive
+    const int r0 = tq * OR, gx = tx0 + tx;
+    float col[OR + 2 * R];
 #pragma unroll
-  for (int i = 0; i < OR + 2 * R; ++i) col[i] = RV[r0 + i][tx];
+    for (int i = 0; i < OR + 2 * R; ++i) col[i] = RV[r0 + i][tx];
 #pragma unroll
-  for (int i = 0; i < OR; ++i) {
-    float b = col[i];
+    for (int i = 0; i < OR; ++i) {
+      float b = col[i];
 #pragma unroll
-    for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, col[i + d]);
-    const int gy = ty0 + r0 + i;
-    if (gy < H && gx < W) yp[(int64_t)gy * W + gx] = b;
+      for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, col[i + d]);
+      const int gy = ty0 + r0 + i;
+      if (gy < H && gx < W) yp[(int64_t)gy * W + gx] = b;
+    }
   }
 }
 
@@ -356,7 +361,7 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restri
 template <bool SUP>
 static bool flat_fwd_fixed(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int ry, int rx, cudaStream_t s) {
   if (ry != rx || ry < 1 || ry > 3 || planes > 65535) return false;
-  const dim3 grid((unsigned)ceil_div(w, AT_W), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
+  const dim3 grid((unsigned)ceil_div(w, AF_TX - 2 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
   if (ry == 1) k_flat_fwd_r<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
   else if (ry == 2) k_flat_fwd_r<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
   else k_flat_fwd_r<SUP, 3><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
