@@ -126,6 +126,22 @@ static pg_status static_iter(const pg_image &in, int se, int iter, const pg_imag
   if (iter < 0) return fail(PG_ERR_INVALID_ARGUMENT, "iter must be >= 0");
   if (iter == 0) return launch_copy(in, out, s);
   if (iter == 1) return launch_small_se(in, out, se, dilate, s);
+  // Iterating a box SE (the 3x3 square, a 3-pixel X or Y segment) `iter` times under the
+  // clipped border equals one pass of the box `iter` times as wide: along each axis every
+  // pixel between two in-image pixels is in the image, so both reach the same pixels.  The
+  // line kernels cost O(1) per pixel instead of O(iter).  On 4096^2 images one X or Y line
+  // pass beats two 3-pixel passes for every type; the square (two line passes) catches up
+  // with the repeated 3x3 pass at 5 iterations for 1- and 2-byte types and at 3 for wider.
+  const int es = elem_size(in.ptype);
+  switch (se) {
+    case PG_SE_SEGMENT_X_1D:
+    case PG_SE_SEGMENT_X_2D: return launch_line(in, out, 0, 1, iter, dilate, s);
+    case PG_SE_SEGMENT_Y_2D: return launch_line(in, out, 1, 0, iter, dilate, s);
+    case PG_SE_SQUARE_2D:
+      if (iter >= (es <= 2 ? 5 : 3)) return launch_rect(in, out, iter, iter, dilate, s);
+      break;
+    default: break;
+  }
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
   pg_image t = in;

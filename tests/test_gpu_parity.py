@@ -82,7 +82,8 @@ def test_static_2d_random(dt, se):
     for shape in SHAPES_2D:
         a = rand(rng, shape, dt)
         x = dev(a)
-        for it in (1, 2, 3):
+        # 1-2 take the repeated 3x3 pass, the rest the line kernels (the square from 3 or 5)
+        for it in (1, 2, 3, 5, 7, 40):
             for dil in (True, False):
                 out = torch.empty_like(x)
                 (llm.Dilate if dil else llm.Erode)(x, Common_NL_SE[se], it, out)
@@ -113,9 +114,12 @@ def test_static_1d(se, dt):
     for n in (1, 2, 15, 16, 17, 1000):
         a = rand(rng, (n,), dt)
         x = dev(a)
-        out = torch.empty_like(x)
-        llm.Dilate(x, Common_NL_SE[se], 2, out)
-        np.testing.assert_array_equal(host(out), oracle.erode_dilate_static(a, se, 2, True))
+        for it in (1, 2, 9):
+            for dil in (True, False):
+                out = torch.empty_like(x)
+                (llm.Dilate if dil else llm.Erode)(x, Common_NL_SE[se], it, out)
+                np.testing.assert_array_equal(host(out), oracle.erode_dilate_static(a, se, it, dil),
+                                              err_msg=f"n={n} iter={it} dilate={dil}")
 
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32])
@@ -219,15 +223,19 @@ def test_rect_and_composites(dt):
             np.testing.assert_array_equal(host(out), exp, err_msg=f"{fn.__name__} {hy}x{hx}")
 
 
-def test_square_iterated_equals_rect_on_gpu():
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.float32])
+def test_square_iterated_equals_rect_on_gpu(dt):
+    # the iterated square runs as a rectangle: check it against the oracle's 15 repeated 3x3
+    # passes on a size where the line kernels take their fast (streaming / word) paths
     from poutre2_gb300 import llm
     from poutre2_gb300.se import Common_NL_SE
     rng = np.random.default_rng(6)
-    a = rand(rng, (100, 90), np.float32)
+    a = rand(rng, (300, 256), dt)
     x = dev(a)
     o1, o2 = torch.empty_like(x), torch.empty_like(x)
     llm.Dilate(x, Common_NL_SE.SESquare2D, 15, o1)
     llm.DilateSE(x, llm.se_rect(15, 15), o2)
+    np.testing.assert_array_equal(host(o1), oracle.erode_dilate_static(a, "SESquare2D", 15, True))
     np.testing.assert_array_equal(host(o1), host(o2))
 
 
