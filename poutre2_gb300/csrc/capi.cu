@@ -121,27 +121,9 @@ static pg_status check_scalar(int ptype, double v, const char *what) {
 }
 
 // ------------------------------------------------------------------ erosion / dilation
-static pg_status static_iter(const pg_image &in, int se, int iter, const pg_image &out, bool dilate, cudaStream_t s) {
-  if (se_rank(se) == 0 || se_rank(se) != in.rank) return fail(PG_ERR_UNSUPPORTED_SE, "unsupported nl_static");
-  if (iter < 0) return fail(PG_ERR_INVALID_ARGUMENT, "iter must be >= 0");
-  if (iter == 0) return launch_copy(in, out, s);
+// `iter` passes of a small static SE, alternating between `out` and a temporary
+static pg_status repeat_small(const pg_image &in, int se, int iter, const pg_image &out, bool dilate, cudaStream_t s) {
   if (iter == 1) return launch_small_se(in, out, se, dilate, s);
-  // Iterating a box SE (the 3x3 square, a 3-pixel X or Y segment) `iter` times under the
-  // clipped border equals one pass of the box `iter` times as wide: along each axis every
-  // pixel between two in-image pixels is in the image, so both reach the same pixels.  The
-  // line kernels cost O(1) per pixel instead of O(iter).  On 4096^2 images one X or Y line
-  // pass beats two 3-pixel passes for every type; the square (two line passes) catches up
-  // with the repeated 3x3 pass at 5 iterations for 1- and 2-byte types and at 3 for wider.
-  const int es = elem_size(in.ptype);
-  switch (se) {
-    case PG_SE_SEGMENT_X_1D:
-    case PG_SE_SEGMENT_X_2D: return launch_line(in, out, 0, 1, iter, dilate, s);
-    case PG_SE_SEGMENT_Y_2D: return launch_line(in, out, 1, 0, iter, dilate, s);
-    case PG_SE_SQUARE_2D:
-      if (iter >= (es <= 2 ? 5 : 3)) return launch_rect(in, out, iter, iter, dilate, s);
-      break;
-    default: break;
-  }
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
   pg_image t = in;
@@ -154,6 +136,37 @@ static pg_status static_iter(const pg_image &in, int se, int iter, const pg_imag
     src = dst;
   }
   return PG_OK;
+}
+
+// Erosion / dilation of a 1D or 2D image by the (2hy+1) x (2hx+1) box (hy = 0: X segment, hx = 0:
+// Y segment).  Iterating the 3x3 square, or a 3-pixel X or Y segment, k times under the clipped
+// border equals one pass of the box k times as wide: along each axis every pixel between two
+// in-image pixels is in the image, so both reach the same pixels.  Whichever form is faster runs.
+// On 4096^2 images a 3-pixel pass costs 10-15 us (1-, 2-byte pixels), a line pass of any length
+// 20-30 us: the square runs as repeated 3x3 passes up to 4 (1-, 2-byte pixels) or 2 (wider),
+// a 3-pixel segment as one 3-pixel pass, anything else as line passes.
+static pg_status box(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s) {
+  const int64_t square_passes_max = elem_size(in.ptype) <= 2 ? 4 : 2;
+  if (hy == 0 && hx == 1)
+    return launch_small_se(in, out, in.rank == 1 ? PG_SE_SEGMENT_X_1D : PG_SE_SEGMENT_X_2D, dilate, s);
+  if (in.rank == 2 && hy == 1 && hx == 0) return launch_small_se(in, out, PG_SE_SEGMENT_Y_2D, dilate, s);
+  if (in.rank == 2 && hy == hx && hy >= 1 && hy <= square_passes_max)
+    return repeat_small(in, PG_SE_SQUARE_2D, (int)hy, out, dilate, s);
+  if (hy == 0) return launch_line(in, out, 0, 1, hx, dilate, s);
+  return launch_rect(in, out, hy, hx, dilate, s);
+}
+
+static pg_status static_iter(const pg_image &in, int se, int iter, const pg_image &out, bool dilate, cudaStream_t s) {
+  if (se_rank(se) == 0 || se_rank(se) != in.rank) return fail(PG_ERR_UNSUPPORTED_SE, "unsupported nl_static");
+  if (iter < 0) return fail(PG_ERR_INVALID_ARGUMENT, "iter must be >= 0");
+  if (iter == 0) return launch_copy(in, out, s);
+  switch (se) {  // the boxes: one pass of the box `iter` times as wide (see box())
+    case PG_SE_SEGMENT_X_1D:
+    case PG_SE_SEGMENT_X_2D: return box(in, out, 0, iter, dilate, s);
+    case PG_SE_SEGMENT_Y_2D: return box(in, out, iter, 0, dilate, s);
+    case PG_SE_SQUARE_2D: return box(in, out, iter, iter, dilate, s);
+    default: return repeat_small(in, se, iter, out, dilate, s);
+  }
 }
 
 // sequence of static passes (compound SEs): passes[i] applied in order
@@ -200,6 +213,15 @@ static pg_status compound(const pg_image &in, int compound_se, int size, const p
   std::vector<int> passes;
   passes.push_back(cross);
   for (int i = 1; i < size - nb_square; ++i) passes.push_back(cross);
+  if (in.rank == 2 && nb_square >= 2) {
+    // the trailing run of squares is one box (see box())
+    Scratch tmp;
+    PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
+    pg_image t = in;
+    t.data = tmp.ptr;
+    PG_TRY(static_sequence(in, passes, t, dilate, s));
+    return box(t, out, nb_square, nb_square, dilate, s);
+  }
   for (int i = 0; i < nb_square; ++i) passes.push_back(square);
   return static_sequence(in, passes, out, dilate, s);
 }
@@ -209,10 +231,13 @@ static pg_status by_se(const pg_image &in, const pg_se &se, const pg_image &out,
     case PG_SE_KIND_STATIC: return static_iter(in, se.common_se, se.iter, out, dilate, s);
     case PG_SE_KIND_RECT:
       if (in.rank != 2) return fail(PG_ERR_UNSUPPORTED_SE, "rectangle SE needs a 2D image");
-      return launch_rect(in, out, se.hy, se.hx, dilate, s);
+      if (se.hy < 0 || se.hx < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative rectangle half size");
+      return box(in, out, se.hy, se.hx, dilate, s);
     case PG_SE_KIND_LINE:
       if (in.rank != 2) return fail(PG_ERR_UNSUPPORTED_SE, "line SE needs a 2D image");
       if (se.half < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative half segment");
+      if (se.dy == 0 && (se.dx == 1 || se.dx == -1)) return box(in, out, 0, se.half, dilate, s);
+      if (se.dx == 0 && (se.dy == 1 || se.dy == -1)) return box(in, out, se.half, 0, dilate, s);
       return launch_line(in, out, se.dy, se.dx, se.half, dilate, s);
     case PG_SE_KIND_NL:
       if (!se.offsets || se.n < 1 || se.n > 4096) return fail(PG_ERR_INVALID_ARGUMENT, "neighbour list must hold 1..4096 offsets");
@@ -307,7 +332,7 @@ static pg_status line_x(const pg_image *in, int64_t half, const pg_image *out, b
   PG_TRY(check_in_out(in, out, what));
   if (in->rank > 2) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + " Unsupported number of dims");
   if (half <= 0) return launch_copy(*in, *out, s);  // size_line_segment <= 0 copies (ero_dil_line_se_t.hpp:161-164)
-  return launch_line(*in, *out, 0, 1, half, dilate, s);
+  return box(*in, *out, 0, half, dilate, s);
 }
 static pg_status line_y(const pg_image *in, int64_t half, const pg_image *out, bool dilate, cudaStream_t s,
                         const char *what) {
@@ -316,7 +341,7 @@ static pg_status line_y(const pg_image *in, int64_t half, const pg_image *out, b
   // t_DilateY transposes into a temporary of the input's shape (ero_dil_line_se_t.hpp:258)
   if (in->shape[0] != in->shape[1]) return fail(PG_ERR_NOT_SQUARE, std::string(what) + " needs a square image (t_transpose)");
   if (half <= 0) return launch_copy(*in, *out, s);
-  return launch_line(*in, *out, 1, 0, half, dilate, s);
+  return box(*in, *out, half, 0, dilate, s);
 }
 pg_status pg_erode_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_x(in, half, out, false, STREAM(s), "ErodeX"); }
 pg_status pg_dilate_x(const pg_image *in, int64_t half, const pg_image *out, pg_stream_t s) { return line_x(in, half, out, true, STREAM(s), "DilateX"); }

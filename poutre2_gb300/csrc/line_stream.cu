@@ -4,7 +4,7 @@
 // Same result as line.cu / line_w.cu for the Y segment of 2K+1 pixels (DilateY/ErodeY,
 // ero_dil_line_se_t.hpp:249-282; clipped window) and for the 45 / 135 degree segments (runtime
 // neighbour lists).  Used for the half lengths instantiated below, 1/2/4-byte pixels, word-aligned
-// rows.
+// rows (the 1-/2-byte diagonals through k_dline_words, which keeps whole words).
 //
 // A thread owns one 32-bit word column (E = 4/sizeof(T) adjacent pixel columns) of a strip of
 // rows and walks down it block by block (blocks of W = 2K+1 rows, anchored K rows above the
@@ -101,6 +101,84 @@ __global__ void __launch_bounds__(kLSThreads) k_dline_stream(const T *__restrict
   }
 }
 
+// Diagonal segments of 1- and 2-byte pixels, E = 4 / sizeof(T) adjacent diagonals per thread.  Lane j
+// of a warp follows the E diagonals through word u = c + j of row y0 (pixels E*u .. E*u + E - 1).  At
+// row y = y0 + d they sit at pixel E*u + s, s = -d (45 degrees) or +d (135 degrees): inside word
+// u + q, q = floor(s / E), shifted by m = s - q*E pixels -- the same q and m for the whole warp.  Each
+// lane loads word u + q and funnel-shifts it with the next lane's word by m pixels.  Results go back
+// the same way: the aligned word u + q holds the last m pixels of lane j - 1 and the first E - m of
+// lane j.  Lane 31 only lends its word to lane 30 and lane 0 only its results to lane 1, so a warp
+// writes the 30 words c + q + 1 .. c + q + 30 of a row, and consecutive warps are 30 words apart.
+// Loads and stores stay whole aligned words; no thread leaves early (the shuffles need every lane).
+template <typename T, bool SUP, int K, int DIR>
+__global__ void __launch_bounds__(kLSThreads) k_dline_words(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                                                           int H, int Wn, int strip, int u_first) {
+  constexpr int W = 2 * K + 1;
+  constexpr int LOG2E = sizeof(T) == 1 ? 2 : 1;
+  constexpr int E = 1 << LOG2E;
+  constexpr int PB = 8 * (int)sizeof(T);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * kLSThreads + threadIdx.x) >> 5);
+  const int u = u_first + warp * 30 + lane - 1;
+  const bool writer = lane >= 1 && lane <= 30;
+  const int y0 = blockIdx.y * strip;
+  const int y1 = min(y0 + strip, H);
+  const uint32_t NEUW = splat<T>(Op<T, SUP>::neutral());
+  uint32_t suf[W];
+#pragma unroll
+  for (int i = 0; i < W; ++i) suf[i] = NEUW;
+  const int ys = y0 - K;
+  for (int yb = ys; yb < y1 + K; yb += W) {
+    uint32_t raw[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int y = yb + i;
+      const int wi = u + ((DIR > 0 ? y0 - y : y - y0) >> LOG2E);
+      raw[i] = (y >= 0 && y < H && wi >= 0 && wi < Wn) ? __ldg(in + (size_t)y * Wn + wi) : NEUW;
+    }
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int m = (DIR > 0 ? y0 - (yb + i) : (yb + i) - y0) & (E - 1);
+      const uint32_t hi = __shfl_down_sync(FULL, raw[i], 1);
+      raw[i] = __funnelshift_r(raw[i], hi, (unsigned)(m * PB));
+    }
+    uint32_t pre = raw[0];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0) pre = wop<T, SUP>(pre, raw[i]);
+      const int y = yb + i - K;
+      const uint32_t r = (i < W - 1) ? wop<T, SUP>(suf[i + 1], pre) : pre;
+      const int s = DIR > 0 ? y0 - y : y - y0;
+      const int m = s & (E - 1);
+      const uint32_t prev = __shfl_up_sync(FULL, r, 1);
+      const uint32_t w = m ? __funnelshift_r(prev, r, (unsigned)((E - m) * PB)) : r;
+      const int wi = u + (s >> LOG2E);
+      if (writer && y >= y0 && y < y1 && wi >= 0 && wi < Wn) out[(size_t)y * Wn + wi] = w;
+    }
+    suf[W - 1] = raw[W - 1];
+#pragma unroll
+    for (int i = W - 2; i >= 0; --i) suf[i] = wop<T, SUP>(suf[i + 1], raw[i]);
+  }
+}
+
+template <typename T, bool SUP, int K, int DIR>
+static void dw_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
+  constexpr int E = 4 / (int)sizeof(T);
+  const int Wn = W / E;
+  // rows of the strip shift the words by q in [qlo, qhi]; the warps' 30-word spans must cover
+  // every word of every row
+  int strip = 256;
+  auto span = [&](int st) { return (int64_t)(st - 1 + E - 1) / E + 1; };  // qhi - qlo + 1 (upper bound)
+  auto ctas_x = [&](int st) { return ceil_div(ceil_div((int64_t)Wn + span(st), 30) * 32, kLSThreads); };
+  while (strip > 32 && ctas_x(strip) * ceil_div(H, strip) < 4LL * num_sms()) strip /= 2;
+  const int qext = (strip - 1 + E - 1) / E;  // |q| over the strip's rows is at most this
+  const int u_first = DIR > 0 ? 0 : -qext;
+  dim3 grid((unsigned)ctas_x(strip), (unsigned)ceil_div(H, strip));
+  k_dline_words<T, SUP, K, DIR><<<grid, kLSThreads, 0, s>>>(reinterpret_cast<const uint32_t *>(in),
+                                                           reinterpret_cast<uint32_t *>(out), H, Wn, strip, u_first);
+}
+
 template <typename T, bool SUP, int K, int DIR>
 static void ds_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
   // threads cover W + strip pixels of row y0: the band drifts left (45) or right (135) by one pixel
@@ -129,7 +207,10 @@ static void vs_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
 template <typename T, bool SUP, int K>
 static void line_launch(const T *in, T *out, int H, int W, int dx, cudaStream_t s) {
   if (dx == 0) vs_launch<T, SUP, K>(in, out, H, W, s);
-  else if (dx == -1) ds_launch<T, SUP, K, 1>(in, out, H, W, s);
+  else if constexpr (sizeof(T) < 4) {
+    if (dx == -1) dw_launch<T, SUP, K, 1>(in, out, H, W, s);
+    else dw_launch<T, SUP, K, -1>(in, out, H, W, s);
+  } else if (dx == -1) ds_launch<T, SUP, K, 1>(in, out, H, W, s);
   else ds_launch<T, SUP, K, -1>(in, out, H, W, s);
 }
 
@@ -152,15 +233,16 @@ bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, in
                      pg_status *st) {
   const int es = elem_size(in.ptype);
   if (es > 4 || dy != 1 || dx < -1 || dx > 1) return false;
-  // diagonals: 4-byte pixels only (for 1- and 2-byte pixels the word-packed staircase tiles of
-  // line_w.cu measured as fast or faster on 4096^2)
-  if (dx != 0 && es != 4) return false;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, W = d.nx;
   if (H < 1 || H > (1 << 30) || W > (1 << 29) || ceil_div(H, 32) > 65535) return false;
-  // the vertical kernel moves whole 32-bit words; the diagonal one single pixels
-  if (dx == 0 && (W * es) % 4 != 0) return false;
-  if (dx == 0 && (reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 4 != 0) return false;
+  // the vertical kernel and the 1-/2-byte diagonal kernel move whole 32-bit words; the 4-byte
+  // diagonal one single pixels
+  // u8 diagonals of 63 pixels: the word kernel's register window (196 registers) leaves too few
+  // warps; the staircase tiles of line_w.cu measured faster there (54 vs 68 us on 4096^2)
+  if (dx != 0 && es == 1 && k > 15) return false;
+  if ((W * es) % 4 != 0) return false;
+  if ((reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 4 != 0) return false;
   bool ok = false;
   switch (in.ptype) {
     case PG_PTYPE_U8: {

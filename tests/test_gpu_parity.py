@@ -191,14 +191,14 @@ def test_lines_xy(dt, half):
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32, np.float64])
 @pytest.mark.parametrize("d", [(0, 1), (1, 0), (-1, 1), (1, 1)])
-@pytest.mark.parametrize("half", [1, 5, 31])
+@pytest.mark.parametrize("half", [1, 3, 5, 7, 31])
 def test_segments_any_direction(dt, d, half):
     from poutre2_gb300 import llm
     from poutre2_gb300.se import NeighborList
     rng = np.random.default_rng(half * 7 + d[0] * 3 + d[1])
     offs = NeighborList.segment(d[0], d[1], half).offsets
     # word-aligned rows for every pixel type (fast path) and a ragged width (fallback)
-    for shape in [(77, 150), (100, 136), (9, 260), (200, 64), (3, 4)]:
+    for shape in [(77, 150), (100, 136), (9, 260), (200, 64), (3, 4), (300, 520)]:
         a = rand(rng, shape, dt)
         x = dev(a)
         for dil in (True, False):
@@ -207,13 +207,14 @@ def test_segments_any_direction(dt, d, half):
             np.testing.assert_array_equal(host(out), oracle.erode_dilate_nl(a, offs, dil), err_msg=f"{shape}")
 
 
-@pytest.mark.parametrize("dt", [np.uint16, np.float32])
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.float32])
 def test_rect_and_composites(dt):
     from poutre2_gb300 import llm
     rng = np.random.default_rng(4)
-    a = rand(rng, (150, 170), dt)
+    a = rand(rng, (150, 172), dt)
     x = dev(a)
-    for hy, hx in ((15, 15), (0, 4), (3, 0), (2, 9)):
+    # squares up to 4 run as repeated 3x3 passes, 3-pixel segments as one 3-pixel pass
+    for hy, hx in ((15, 15), (0, 4), (3, 0), (2, 9), (1, 1), (2, 2), (3, 3), (4, 4), (5, 5), (0, 1), (1, 0)):
         se = llm.se_rect(hy, hx)
         d, e = oracle.rect(a, hy, hx, True), oracle.rect(a, hy, hx, False)
         for fn, exp in ((llm.DilateSE, d), (llm.ErodeSE, e), (llm.Opening, oracle.rect(e, hy, hx, True)),
