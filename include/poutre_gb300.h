@@ -239,10 +239,11 @@ PG_API pg_status pg_flat_morph2d_backward(const float *x, const float *grad_out,
 PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const pg_image *mask,
                                            int32_t common_se, const pg_image *out, pg_stream_t stream);
 
-/* Synchronises `stream`, then returns (and clears) the device-side status of the geodesy
- * kernels: PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device
- * wait) since the last check, else PG_OK.  The geodesy calls above are asynchronous; call this
- * to observe the failure the reference would have thrown. */
+/* Synchronises `stream`, then returns (and clears) the device-side status of the kernels:
+ * PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device wait), or
+ * PG_ERR_CUDA when a one-pass square erosion / dilation found a tile load unfinished after its
+ * bounded wait, since the last check; else PG_OK.  The calls are asynchronous; call this to
+ * observe the failure the reference would have thrown. */
 PG_API pg_status pg_check_device(pg_stream_t stream);
 
 /* Passes of the last completed reconstruction on the current device (diagnostics; synchronises

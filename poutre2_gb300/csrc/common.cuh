@@ -192,6 +192,9 @@ bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, in
 bool try_line_words(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
                     pg_status *st);
 pg_status launch_rect(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s);
+bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
+                    pg_status *st);
+int take_rect_status();  // device status of the fused square kernel since the last call (0: none)
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
 pg_status launch_sat_const(const pg_image &in, double v, bool add, const pg_image &out, cudaStream_t s);

@@ -35,14 +35,16 @@ __global__ void __launch_bounds__(kLSThreads) k_vline_stream(const uint32_t *__r
   uint32_t suf[W];  // running suffix of the previous block
 #pragma unroll
   for (int i = 0; i < W; ++i) suf[i] = NEUW;
-  // blocks start at ys = y0 - K; block b covers rows [ys + b*W, ys + (b+1)*W)
+  // blocks start at ys = y0 - K; block b covers rows [ys + b*W, ys + (b+1)*W); rows from y1 + K on
+  // only feed outputs below the strip and are not read
   const int ys = y0 - K;
+  const int ylim = min(y1 + K, H);
   for (int yb = ys; yb < y1 + K; yb += W) {
     uint32_t raw[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) {
       const int y = yb + i;
-      raw[i] = (y >= 0 && y < H) ? __ldg(src + (size_t)y * Wn) : NEUW;
+      raw[i] = (y >= 0 && y < ylim) ? __ldg(src + (size_t)y * Wn) : NEUW;
     }
     // prefix of this block; the output row y = yb + i - K uses suf[i + 1] (previous block's
     // suffix at y - K) and the prefix at y + K; for i = W-1 the window is exactly this block
@@ -129,13 +131,14 @@ __global__ void __launch_bounds__(kLSThreads) k_dline_words(const uint32_t *__re
 #pragma unroll
   for (int i = 0; i < W; ++i) suf[i] = NEUW;
   const int ys = y0 - K;
+  const int ylim = min(y1 + K, H);  // rows below only feed outputs below the strip
   for (int yb = ys; yb < y1 + K; yb += W) {
     uint32_t raw[W];
 #pragma unroll
     for (int i = 0; i < W; ++i) {
       const int y = yb + i;
       const int wi = u + ((DIR > 0 ? y0 - y : y - y0) >> LOG2E);
-      raw[i] = (y >= 0 && y < H && wi >= 0 && wi < Wn) ? __ldg(in + (size_t)y * Wn + wi) : NEUW;
+      raw[i] = (y >= 0 && y < ylim && wi >= 0 && wi < Wn) ? __ldg(in + (size_t)y * Wn + wi) : NEUW;
     }
 #pragma unroll
     for (int i = 0; i < W; ++i) {
@@ -167,11 +170,13 @@ static void dw_launch(const T *in, T *out, int H, int W, cudaStream_t s) {
   constexpr int E = 4 / (int)sizeof(T);
   const int Wn = W / E;
   // rows of the strip shift the words by q in [qlo, qhi]; the warps' 30-word spans must cover
-  // every word of every row
-  int strip = 256;
+  // every word of every row.  Strips of about 8K rows keep the 2K-row halo small (measured on
+  // 4096^2: 256 rows for K = 31, 128 for 15, 64 for 3), shorter ones only for small images.
+  int strip = 64;
+  while (strip < 512 && strip < 8 * K) strip *= 2;
   auto span = [&](int st) { return (int64_t)(st - 1 + E - 1) / E + 1; };  // qhi - qlo + 1 (upper bound)
   auto ctas_x = [&](int st) { return ceil_div(ceil_div((int64_t)Wn + span(st), 30) * 32, kLSThreads); };
-  while (strip > 32 && ctas_x(strip) * ceil_div(H, strip) < 4LL * num_sms()) strip /= 2;
+  while (strip > 32 && ctas_x(strip) * ceil_div(H, strip) < 2LL * num_sms()) strip /= 2;
   const int qext = (strip - 1 + E - 1) / E;  // |q| over the strip's rows is at most this
   const int u_first = DIR > 0 ? 0 : -qext;
   dim3 grid((unsigned)ctas_x(strip), (unsigned)ceil_div(H, strip));

@@ -1604,6 +1604,8 @@ pg_status pg_check_device(pg_stream_t stream) {
     PG_CUDA_TRY(cudaMemcpyToSymbol(pg::g_recon_status, &zero, sizeof(int)), "clear device status");
     return pg::fail(static_cast<pg_status>(st), "reconstruction did not converge within its round cap or wait limit");
   }
+  if (const int rs = pg::take_rect_status())
+    return pg::fail(static_cast<pg_status>(rs), "a square tile load did not complete within its wait limit");
   return PG_OK;
 }
 
