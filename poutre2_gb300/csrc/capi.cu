@@ -152,9 +152,9 @@ static pg_status box(const pg_image &in, const pg_image &out, int64_t hy, int64_
   if (in.rank == 2 && hy == 1 && hx == 0) return launch_small_se(in, out, PG_SE_SEGMENT_Y_2D, dilate, s);
   if (in.rank == 2 && hy == hx && hy >= 1 && hy <= square_passes_max)
     return repeat_small(in, PG_SE_SQUARE_2D, (int)hy, out, dilate, s);
-  if (hy == 0) return launch_line(in, out, 0, 1, hx, dilate, s);
   pg_status st = PG_OK;
-  if (try_rect_fused(in, out, hy, hx, dilate, s, &st)) return st;  // one-pass square (rect.cu)
+  if (try_rect_fused(in, out, hy, hx, dilate, s, &st)) return st;  // shared-memory tile pass (rect.cu)
+  if (hy == 0) return launch_line(in, out, 0, 1, hx, dilate, s);
   return launch_rect(in, out, hy, hx, dilate, s);
 }
 

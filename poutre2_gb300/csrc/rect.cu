@@ -1,10 +1,12 @@
-// rect.cu -- erosion / dilation by the (2K+1) x (2K+1) square (K = 7, 15, 31) in one pass.
+// rect.cu -- erosion / dilation by the (2KY+1) x (2KX+1) box in one pass through shared memory: the
+// square (KY = KX), the X segment (KY = 0) and the Y segment (KX = 0), for K = 7, 15, 31.
 //
-// Same result as the separable pair of line passes of line.cu (DilateX then DilateY over a clipped
-// window; the square is the Minkowski sum of an X and a Y segment, so the order is immaterial): one
-// tile is read once and written once instead of the two round trips of the separable form.
+// Same result as the separable line passes of line.cu (DilateX then DilateY over a clipped window;
+// the box is the Minkowski sum of an X and a Y segment, so the order is immaterial): one tile is read
+// once and written once instead of the two round trips of the separable form, and one TMA copy per
+// tile keeps a whole tile's loads in flight where the streaming kernels are limited by latency.
 //
-// A CTA (128 threads) owns an output tile of TH = 128 - 2K rows by TW = 64 or 32 centre 32-bit words
+// A CTA (128 threads) owns an output tile of TH = 128 - 2KY rows by TW = 64 or 32 centre 32-bit words
 // (E = 4 / sizeof(T) pixels per word).  One TMA copy (cp.async.bulk.tensor.2d, completion on an
 // mbarrier) brings the 128 input rows of the tile plus HW halo words each side into shared memory;
 // pixels outside the image are then set to the neutral value.  Row pass: thread r runs van Herk /
@@ -13,7 +15,8 @@
 // so the 8 threads of a shared-memory phase touch 8 distinct chunks).  Column pass: the 128 threads
 // split into 128 / TW row groups of TW centre columns; each runs the same scan down its column over
 // its group's rows (SIMD within the word: 2 x u16 or 4 x u8 min/max) and writes the output rows
-// straight to global memory, a warp covering 32 consecutive words of a row.
+// straight to global memory, a warp covering 32 consecutive words of a row (for KY = 0 the centre
+// words are copied out; for KX = 0 there is no row pass).
 //
 // The wait on the mbarrier is bounded (kRectWaitNs of %globaltimer); on expiry the CTA records
 // PG_ERR_CUDA in g_rect_status (read by pg_check_device) and leaves its tile unwritten.
@@ -34,16 +37,16 @@ namespace {
 constexpr int kRThreads = 128;                             // = input rows per tile
 constexpr unsigned long long kRectWaitNs = 1000000000ull;  // 1 s
 
-template <typename T, int K> struct RectGeom {
+template <typename T, int KY, int KX> struct RectGeom {
   static constexpr int E = 4 / (int)sizeof(T);
-  // centre words: 64, or 32 for K = 31 (measured on 4096^2: the tile's shared memory sets the CTAs
-  // per SM, and the row pass's share of halo work grows with K)
-  static constexpr int TW = K >= 31 ? 32 : 64;
-  static constexpr int HW = ((K + E - 1) / E + 3) / 4 * 4;      // halo words per side, whole 16-byte chunks
+  // centre words: 64, or 32 for KX = 31 (measured on 4096^2: the tile's shared memory sets the CTAs
+  // per SM, and the row pass's share of halo work grows with KX)
+  static constexpr int TW = KX >= 31 ? 32 : 64;
+  static constexpr int HW = ((KX + E - 1) / E + 3) / 4 * 4;     // halo words per side, whole 16-byte chunks
   static constexpr int BW0 = TW + 2 * HW;
   static constexpr int BW = ((BW0 / 4) & 1) ? BW0 : BW0 + 4;    // row pitch: an odd number of 16-byte chunks
   static constexpr int TR = kRThreads;                          // input rows per tile
-  static constexpr int TH = TR - 2 * K;                         // output rows per tile
+  static constexpr int TH = TR - 2 * KY;                        // output rows per tile
   static constexpr int NV = kRThreads / TW;                     // column-pass row groups
   static constexpr int THG = (TH + NV - 1) / NV;                // output rows per group
   static constexpr size_t tile_bytes = (size_t)TR * BW * 4;
@@ -79,12 +82,11 @@ template <typename T> __device__ __forceinline__ uint32_t bits_of(T v) {
   else return (uint32_t)v;
 }
 
-template <typename T, bool SUP, int K>
-__global__ void __launch_bounds__(kRThreads) k_rect_fused(const __grid_constant__ CUtensorMap tmap,
+template <typename T, bool SUP, int KY, int KX>
+__global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_constant__ CUtensorMap tmap,
                                                           uint32_t *__restrict__ out, int H, int Wn) {
-  using G = RectGeom<T, K>;
+  using G = RectGeom<T, KY, KX>;
   constexpr int E = G::E, HW = G::HW, BW = G::BW, TR = G::TR, TH = G::TH, TW = G::TW, THG = G::THG;
-  constexpr int W = 2 * K + 1;
   using O = Op<T, SUP>;
   extern __shared__ __align__(128) uint32_t s_tile[];
   __shared__ int s_ok;
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(kRThreads) k_rect_fused(const __grid_constant_
   const int t = threadIdx.x;
   const int wx0 = blockIdx.x * TW;         // first centre word
   const int y0 = blockIdx.y * TH;          // first output row
-  const int tx = wx0 - HW, ty = y0 - K;    // tile origin: word, row (a multiple of 4 words)
+  const int tx = wx0 - HW, ty = y0 - KY;   // tile origin: word (a multiple of 4), row
 
   if (t == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
@@ -127,8 +129,9 @@ __global__ void __launch_bounds__(kRThreads) k_rect_fused(const __grid_constant_
   }
 
   // ---- row pass: thread t scans input row t; stream pixel q is tile pixel P0 + q, output pixel j
-  // (tile pixel HW*E + j) is formed at q = j + 2K
-  {
+  // (tile pixel HW*E + j) is formed at q = j + 2KX
+  if constexpr (KX > 0) {
+    constexpr int K = KX, W = 2 * K + 1;
     uint32_t *row = s_tile + t * BW;
     constexpr int NQ = TW * E + 2 * K;
     constexpr int NB = (NQ + W - 1) / W;
@@ -173,15 +176,21 @@ __global__ void __launch_bounds__(kRThreads) k_rect_fused(const __grid_constant_
 #pragma unroll
       for (int i = W - 2; i >= 0; --i) suf[i] = O::apply(suf[i + 1], raw[i]);
     }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- column pass: thread t scans centre word column HW + t % TW over the rows of output group
-  // t / TW (THG output rows, from tile row j0); output row j0 + j is formed at q = j + 2K
-  {
-    const int j0 = (t / TW) * THG;
-    const uint32_t *col = s_tile + j0 * BW + HW + t % TW;
-    const int gx = wx0 + t % TW;
+  // t / TW (THG output rows, from tile row j0); output row j0 + j is formed at q = j + 2KY.  Without
+  // a vertical extent the centre words are copied out.
+  const int j0 = (t / TW) * THG;
+  const uint32_t *col = s_tile + j0 * BW + HW + t % TW;
+  const int gx = wx0 + t % TW;
+  if constexpr (KY == 0) {
+    if (gx < Wn)
+#pragma unroll 4
+      for (int j = 0; j < THG && j0 + j < TH && y0 + j0 + j < H; ++j) out[(size_t)(y0 + j0 + j) * Wn + gx] = col[j * BW];
+  } else {
+    constexpr int K = KY, W = 2 * K + 1;
     const uint32_t NEUW = splat<T>(O::neutral());
     constexpr int NB = (THG + 2 * K + W - 1) / W;
     uint32_t suf[W];
@@ -227,9 +236,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
   return fn;
 }
 
-template <typename T, bool SUP, int K>
+template <typename T, bool SUP, int KY, int KX>
 pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
-  using G = RectGeom<T, K>;
+  using G = RectGeom<T, KY, KX>;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, Wn = d.nx / G::E;
   auto fn = encode_tiled();
@@ -245,19 +254,34 @@ pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
   if (r != CUDA_SUCCESS) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the rectangle tile");
   static std::once_flag attr;
   std::call_once(attr, [] {
-    cudaFuncSetAttribute(k_rect_fused<T, SUP, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
+    cudaFuncSetAttribute(k_rect_fused<T, SUP, KY, KX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
   });
   const dim3 grid((unsigned)ceil_div(Wn, G::TW), (unsigned)ceil_div(H, G::TH));
-  k_rect_fused<T, SUP, K><<<grid, kRThreads, G::smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H, (int)Wn);
-  return cuda_status(cudaGetLastError(), "fused square launch");
+  k_rect_fused<T, SUP, KY, KX><<<grid, kRThreads, G::smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H, (int)Wn);
+  return cuda_status(cudaGetLastError(), "tile erosion / dilation launch");
 }
 
+// (hy, hx): (k, k) square, (0, k) X segment, (k, 0) Y segment, k in {7, 15, 31}
 template <typename T, bool SUP>
-pg_status rect_fused_k(const pg_image &in, const pg_image &out, int k, cudaStream_t s) {
-  switch (k) {
-    case 7: return rect_fused<T, SUP, 7>(in, out, s);
-    case 15: return rect_fused<T, SUP, 15>(in, out, s);
-    default: return rect_fused<T, SUP, 31>(in, out, s);
+pg_status rect_fused_k(const pg_image &in, const pg_image &out, int hy, int hx, cudaStream_t s) {
+  if (hy == hx) {
+    switch (hy) {
+      case 7: return rect_fused<T, SUP, 7, 7>(in, out, s);
+      case 15: return rect_fused<T, SUP, 15, 15>(in, out, s);
+      default: return rect_fused<T, SUP, 31, 31>(in, out, s);
+    }
+  }
+  if (hy == 0) {
+    switch (hx) {
+      case 7: return rect_fused<T, SUP, 0, 7>(in, out, s);
+      case 15: return rect_fused<T, SUP, 0, 15>(in, out, s);
+      default: return rect_fused<T, SUP, 0, 31>(in, out, s);
+    }
+  }
+  switch (hy) {
+    case 7: return rect_fused<T, SUP, 7, 0>(in, out, s);
+    case 15: return rect_fused<T, SUP, 15, 0>(in, out, s);
+    default: return rect_fused<T, SUP, 31, 0>(in, out, s);
   }
 }
 
@@ -265,7 +289,8 @@ pg_status rect_fused_k(const pg_image &in, const pg_image &out, int k, cudaStrea
 
 bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
                     pg_status *st) {
-  if (in.rank != 2 || hy != hx || (hy != 7 && hy != 15 && hy != 31)) return false;
+  auto ok_k = [](int64_t k) { return k == 7 || k == 15 || k == 31; };
+  if (in.rank != 2 || !((hy == hx && ok_k(hy)) || (hy == 0 && ok_k(hx)) || (hx == 0 && ok_k(hy)))) return false;
   const int es = elem_size(in.ptype);
   // 2- and 4-byte pixels (for u8 the row pass's register window spills; the two line passes run)
   if (es != 2 && es != 4) return false;
@@ -273,17 +298,17 @@ bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t
   const int64_t H = d.ny, Wd = d.nx;
   if (H < 1 || Wd < 1 || (Wd * es) % 16 != 0) return false;
   if ((reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 16 != 0) return false;
-  const int k = (int)hy;
-  if (H > (1 << 30) || Wd * es / 4 > (1 << 30) || ceil_div(H, kRThreads - 2 * k) > 65535) return false;
+  if (H > (1 << 30) || Wd * es / 4 > (1 << 30) || ceil_div(H, kRThreads - 2 * hy) > 65535) return false;
+  const int y = (int)hy, x = (int)hx;
   switch (in.ptype) {
     case PG_PTYPE_U16:
-      *st = dilate ? rect_fused_k<uint16_t, true>(in, out, k, s) : rect_fused_k<uint16_t, false>(in, out, k, s);
+      *st = dilate ? rect_fused_k<uint16_t, true>(in, out, y, x, s) : rect_fused_k<uint16_t, false>(in, out, y, x, s);
       return true;
     case PG_PTYPE_I32:
-      *st = dilate ? rect_fused_k<int32_t, true>(in, out, k, s) : rect_fused_k<int32_t, false>(in, out, k, s);
+      *st = dilate ? rect_fused_k<int32_t, true>(in, out, y, x, s) : rect_fused_k<int32_t, false>(in, out, y, x, s);
       return true;
     case PG_PTYPE_F32:
-      *st = dilate ? rect_fused_k<float, true>(in, out, k, s) : rect_fused_k<float, false>(in, out, k, s);
+      *st = dilate ? rect_fused_k<float, true>(in, out, y, x, s) : rect_fused_k<float, false>(in, out, y, x, s);
       return true;
     default: return false;
   }

@@ -226,19 +226,21 @@ def test_rect_and_composites(dt):
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32])
 @pytest.mark.parametrize("k", [7, 15, 31])
-def test_square_one_pass(dt, k):
-    # 15x15, 31x31 and 63x63 squares on rows of a multiple of 16 bytes take the one-pass tile kernel:
-    # images smaller than a tile, several tiles across and down, a 1-row image, and (fallback) a
-    # ragged row width
+@pytest.mark.parametrize("form", ["square", "x", "y"])
+def test_square_one_pass(dt, k, form):
+    # 15x15, 31x31 and 63x63 squares and X / Y segments on rows of a multiple of 16 bytes take the
+    # shared-memory tile kernel: images smaller than a tile, several tiles across and down, a 1-row
+    # image, and (fallback) a ragged row width
     from poutre2_gb300 import llm
+    hy, hx = {"square": (k, k), "x": (0, k), "y": (k, 0)}[form]
     rng = np.random.default_rng(k * 11 + np.dtype(dt).itemsize)
     for shape in [(5, 8), (1, 16), (70, 40), (300, 264), (260, 1000), (131, 520), (97, 30), (40, 2064)]:
         a = rand(rng, shape, dt)
         x = dev(a)
         for dil in (True, False):
             out = torch.empty_like(x)
-            (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_rect(k, k), out)
-            np.testing.assert_array_equal(host(out), oracle.rect(a, k, k, dil), err_msg=f"{shape} dilate={dil}")
+            (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_rect(hy, hx), out)
+            np.testing.assert_array_equal(host(out), oracle.rect(a, hy, hx, dil), err_msg=f"{shape} dilate={dil}")
     import ctypes
     from poutre2_gb300 import _lib
     _lib.call("pg_check_device", ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))  # raises on a device error
