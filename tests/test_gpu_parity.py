@@ -191,14 +191,14 @@ def test_lines_xy(dt, half):
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.float32, np.float64])
 @pytest.mark.parametrize("d", [(0, 1), (1, 0), (-1, 1), (1, 1)])
-@pytest.mark.parametrize("half", [1, 3, 5, 7, 31])
+@pytest.mark.parametrize("half", [1, 3, 5, 7, 15, 31])
 def test_segments_any_direction(dt, d, half):
     from poutre2_gb300 import llm
     from poutre2_gb300.se import NeighborList
     rng = np.random.default_rng(half * 7 + d[0] * 3 + d[1])
     offs = NeighborList.segment(d[0], d[1], half).offsets
     # word-aligned rows for every pixel type (fast path) and a ragged width (fallback)
-    for shape in [(77, 150), (100, 136), (9, 260), (200, 64), (3, 4), (300, 520)]:
+    for shape in [(77, 150), (100, 136), (9, 260), (200, 64), (3, 4), (300, 520), (150, 1032)]:
         a = rand(rng, shape, dt)
         x = dev(a)
         for dil in (True, False):
