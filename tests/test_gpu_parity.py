@@ -237,10 +237,14 @@ def test_square_one_pass(dt, k, form):
     for shape in [(5, 8), (1, 16), (70, 40), (300, 264), (260, 1000), (131, 520), (97, 30), (40, 2064)]:
         a = rand(rng, shape, dt)
         x = dev(a)
+        d, e = oracle.rect(a, hy, hx, True), oracle.rect(a, hy, hx, False)
         for dil in (True, False):
             out = torch.empty_like(x)
             (llm.DilateSE if dil else llm.ErodeSE)(x, llm.se_rect(hy, hx), out)
-            np.testing.assert_array_equal(host(out), oracle.rect(a, hy, hx, dil), err_msg=f"{shape} dilate={dil}")
+            np.testing.assert_array_equal(host(out), d if dil else e, err_msg=f"{shape} dilate={dil}")
+        out = torch.empty_like(x)
+        llm.Gradient(x, llm.se_rect(hy, hx), out)
+        np.testing.assert_array_equal(host(out), (d - e).astype(a.dtype), err_msg=f"{shape} gradient")
     import ctypes
     from poutre2_gb300 import _lib
     _lib.call("pg_check_device", ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))  # raises on a device error
