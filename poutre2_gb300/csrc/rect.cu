@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -252,10 +253,17 @@ pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the rectangle tile");
-  static std::once_flag attr;
-  std::call_once(attr, [] {
-    cudaFuncSetAttribute(k_rect_fused<T, SUP, KY, KX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::smem);
-  });
+  // the opt-in shared-memory size is a per-device attribute of each instantiation
+  static std::atomic<uint64_t> attr_devices{0};
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(attr_devices.load() & bit)) {
+    PG_CUDA_TRY(cudaFuncSetAttribute(k_rect_fused<T, SUP, KY, KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)G::smem),
+                "tile kernel smem attribute");
+    attr_devices.fetch_or(bit);
+  }
   const dim3 grid((unsigned)ceil_div(Wn, G::TW), (unsigned)ceil_div(H, G::TH));
   k_rect_fused<T, SUP, KY, KX><<<grid, kRThreads, G::smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H, (int)Wn);
   return cuda_status(cudaGetLastError(), "tile erosion / dilation launch");
