@@ -249,7 +249,31 @@ static pg_status by_se(const pg_image &in, const pg_se &se, const pg_image &out,
 }
 
 enum Composite { C_OPEN, C_CLOSE, C_GRAD };
+// the box (hy, hx) an SE stands for (see box()), if it is one
+static bool se_box(const pg_se &se, int rank, int64_t &hy, int64_t &hx) {
+  if (rank != 2) return false;
+  switch (se.kind) {
+    case PG_SE_KIND_RECT: hy = se.hy; hx = se.hx; return hy >= 0 && hx >= 0;
+    case PG_SE_KIND_LINE:
+      if (se.half < 0) return false;
+      if (se.dy == 0 && (se.dx == 1 || se.dx == -1)) { hy = 0; hx = se.half; return true; }
+      if (se.dx == 0 && (se.dy == 1 || se.dy == -1)) { hy = se.half; hx = 0; return true; }
+      return false;
+    case PG_SE_KIND_STATIC:
+      if (se.iter < 1) return false;
+      if (se.common_se == PG_SE_SQUARE_2D) { hy = hx = se.iter; return true; }
+      if (se.common_se == PG_SE_SEGMENT_X_2D) { hy = 0; hx = se.iter; return true; }
+      if (se.common_se == PG_SE_SEGMENT_Y_2D) { hy = se.iter; hx = 0; return true; }
+      return false;
+    default: return false;
+  }
+}
+
 static pg_status composite(const pg_image &in, const pg_se &se, const pg_image &out, Composite c, cudaStream_t s) {
+  int64_t hy = 0, hx = 0;
+  pg_status st = PG_OK;
+  // the gradient of a box: dilation and erosion of one tile in one pass (rect.cu)
+  if (c == C_GRAD && se_box(se, in.rank, hy, hx) && try_rect_gradient(in, out, hy, hx, s, &st)) return st;
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
   pg_image t = in;

@@ -192,8 +192,12 @@ bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, in
 bool try_line_words(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
                     pg_status *st);
 pg_status launch_rect(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s);
+// One-pass box (rect.cu): (hy, hx) = (k, k), (0, k) or (k, 0), k in {7, 15, 31}; 2-/4-byte pixels,
+// rows of a multiple of 16 bytes.  try_rect_gradient: dilation - erosion in the same pass.
+bool rect_fused_ok(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool grad);
 bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
                     pg_status *st);
+bool try_rect_gradient(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, cudaStream_t s, pg_status *st);
 int take_rect_status();  // device status of the fused square kernel since the last call (0: none)
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);

@@ -18,6 +18,12 @@
 // straight to global memory, a warp covering 32 consecutive words of a row (for KY = 0 the centre
 // words are copied out; for KX = 0 there is no row pass).
 //
+// Gradient mode (GRAD): the same tile gives the dilation and the erosion at once -- the row pass keeps
+// both running scans and writes the X-eroded centre words to a second shared array, the column pass
+// scans both and stores dilation - erosion -- so the gradient costs one read and one write of the
+// image.  Pixels outside the image then repeat the nearest image pixel instead of a neutral value (a
+// clipped box window contains that pixel, so neither extremum changes).
+//
 // The wait on the mbarrier is bounded (kRectWaitNs of %globaltimer); on expiry the CTA records
 // PG_ERR_CUDA in g_rect_status (read by pg_check_device) and leaves its tile unwritten.
 #include <cuda.h>
@@ -38,7 +44,7 @@ namespace {
 constexpr int kRThreads = 128;                             // = input rows per tile
 constexpr unsigned long long kRectWaitNs = 1000000000ull;  // 1 s
 
-template <typename T, int KY, int KX> struct RectGeom {
+template <typename T, int KY, int KX, bool GRAD> struct RectGeom {
   static constexpr int E = 4 / (int)sizeof(T);
   // centre words: 64, or 32 for KX = 31 (measured on 4096^2: the tile's shared memory sets the CTAs
   // per SM, and the row pass's share of halo work grows with KX)
@@ -50,9 +56,12 @@ template <typename T, int KY, int KX> struct RectGeom {
   static constexpr int TH = TR - 2 * KY;                        // output rows per tile
   static constexpr int NV = kRThreads / TW;                     // column-pass row groups
   static constexpr int THG = (TH + NV - 1) / NV;                // output rows per group
+  // gradient with a row pass: the X-eroded centre words get their own rows (odd chunk count)
+  static constexpr int MP = (GRAD && KX > 0) ? TW + 4 : 0;
   static constexpr size_t tile_bytes = (size_t)TR * BW * 4;
-  static constexpr size_t smem = tile_bytes + 16;               // + the mbarrier
+  static constexpr size_t smem = tile_bytes + (size_t)TR * MP * 4 + 16;  // + the mbarrier
   static_assert(BW <= 256 && TH > 0 && kRThreads % TW == 0, "tile geometry");
+  static_assert(!GRAD || !(KY > 15 && KX > 0), "gradient: register window too large");
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -78,20 +87,147 @@ template <typename T> __device__ __forceinline__ T px_of(uint32_t w, int k) {
   else if constexpr (sizeof(T) == 4) return (T)w;
   else return (T)(w >> (8 * (int)sizeof(T) * k));
 }
+// a - b per pixel of a word, where a >= b in every pixel (a dilation minus an erosion): packed
+// unsigned pixels never borrow from the next lane, so one 32-bit subtraction is exact; i32 wraps like
+// the difference kernel's int arithmetic; f32 is one rounded subtraction, as there
+template <typename T> __device__ __forceinline__ uint32_t wdiff(uint32_t a, uint32_t b) {
+  if constexpr (std::is_same_v<T, float>) return __float_as_uint(__uint_as_float(a) - __uint_as_float(b));
+  else return a - b;
+}
 template <typename T> __device__ __forceinline__ uint32_t bits_of(T v) {
   if constexpr (std::is_same_v<T, float>) return __float_as_uint(v);
   else return (uint32_t)v;
 }
 
-template <typename T, bool SUP, int KY, int KX>
+// Row scan of one tile row (registers), in place: stream pixel q is tile pixel P0 + q, output
+// pixel j (tile pixel HW*E + j) is formed at q = j + 2K.  With GRAD both the dilation (in place) and
+// the erosion (into `mrow`) are formed from the same pixels.
+template <typename T, bool SUP, int K, int TW, int HW, bool GRAD>
+__device__ __forceinline__ void row_scan(uint32_t *row, uint32_t *mrow) {
+  constexpr int E = 4 / (int)sizeof(T), W = 2 * K + 1;
+  constexpr int NQ = TW * E + 2 * K, NB = (NQ + W - 1) / W, P0 = HW * E - K;
+  constexpr int CH = 4 * E;  // pixels per 16-byte chunk
+  using A = Op<T, GRAD ? true : SUP>;
+  using B = Op<T, false>;
+  T sa[W], sb[GRAD ? W : 1];
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    sa[i] = A::neutral();
+    if constexpr (GRAD) sb[i] = B::neutral();
+  }
+  uint32_t cw[4] = {0, 0, 0, 0}, acca[4] = {0, 0, 0, 0}, accb[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    T raw[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int q = b * W + i;
+      if (q < NQ) {
+        const int p = P0 + q;
+        if (q == 0 || p % CH == 0) {
+          const uint4 v = *reinterpret_cast<const uint4 *>(row + (p / CH) * 4);
+          cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
+        }
+        raw[i] = px_of<T>(cw[(p / E) % 4], p % E);
+      } else {
+        raw[i] = A::neutral();  // beyond the stream: feeds no output
+      }
+    }
+    T pa = raw[0], pb = raw[0];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0) {
+        pa = A::apply(pa, raw[i]);
+        if constexpr (GRAD) pb = B::apply(pb, raw[i]);
+      }
+      const int j = b * W + i - 2 * K;
+      if (j >= 0 && j < TW * E) {
+        const int sh = 8 * (int)sizeof(T) * (j % E), wi = (j / E) % 4;
+        const uint32_t va = bits_of<T>((i < W - 1) ? A::apply(sa[i + 1], pa) : pa);
+        acca[wi] = (j % E == 0) ? va : (acca[wi] | (va << sh));
+        if constexpr (GRAD) {
+          const uint32_t vb = bits_of<T>((i < W - 1) ? B::apply(sb[i + 1], pb) : pb);
+          accb[wi] = (j % E == 0) ? vb : (accb[wi] | (vb << sh));
+        }
+        if (j % CH == CH - 1) {
+          *reinterpret_cast<uint4 *>(row + HW + (j / CH) * 4) = make_uint4(acca[0], acca[1], acca[2], acca[3]);
+          if constexpr (GRAD)
+            *reinterpret_cast<uint4 *>(mrow + (j / CH) * 4) = make_uint4(accb[0], accb[1], accb[2], accb[3]);
+        }
+      }
+    }
+    sa[W - 1] = raw[W - 1];
+    if constexpr (GRAD) sb[W - 1] = raw[W - 1];
+#pragma unroll
+    for (int i = W - 2; i >= 0; --i) {
+      sa[i] = A::apply(sa[i + 1], raw[i]);
+      if constexpr (GRAD) sb[i] = B::apply(sb[i + 1], raw[i]);
+    }
+  }
+}
+
+// Column scan of THG output rows (registers) from words `ca` (stride SA) -- and, with GRAD, the
+// erosion from `cb` (stride SB) -- written to out[row y0 + j0 + j][gx] (GRAD: dilation - erosion).
+template <typename T, bool SUP, int K, int THG, int TH, int TR, int SA, int SB, bool GRAD>
+__device__ __forceinline__ void col_scan(const uint32_t *ca, const uint32_t *cb, uint32_t *__restrict__ out,
+                                         int j0, int y0, int gx, int H, int Wn) {
+  constexpr int W = 2 * K + 1, NB = (THG + 2 * K + W - 1) / W;
+  constexpr bool SUPA = GRAD ? true : SUP;
+  const uint32_t NA = splat<T>(Op<T, SUPA>::neutral()), NBW = splat<T>(Op<T, false>::neutral());
+  uint32_t sa[W], sb[GRAD ? W : 1];
+#pragma unroll
+  for (int i = 0; i < W; ++i) {
+    sa[i] = NA;
+    if constexpr (GRAD) sb[i] = NBW;
+  }
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    uint32_t ra[W], rb[GRAD ? W : 1];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int q = b * W + i;
+      const bool in = q < THG + 2 * K && j0 + q < TR;
+      ra[i] = in ? ca[q * SA] : NA;
+      if constexpr (GRAD) rb[i] = in ? cb[q * SB] : NBW;
+    }
+    uint32_t pa = ra[0], pb = 0u;
+    if constexpr (GRAD) pb = rb[0];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0) {
+        pa = wop<T, SUPA>(pa, ra[i]);
+        if constexpr (GRAD) pb = wop<T, false>(pb, rb[i]);
+      }
+      const int j = b * W + i - 2 * K;
+      if (j >= 0 && j < THG && j0 + j < TH) {
+        const int gy = y0 + j0 + j;
+        if (gy < H && gx < Wn) {
+          uint32_t v = (i < W - 1) ? wop<T, SUPA>(sa[i + 1], pa) : pa;
+          if constexpr (GRAD) v = wdiff<T>(v, (i < W - 1) ? wop<T, false>(sb[i + 1], pb) : pb);
+          out[(size_t)gy * Wn + gx] = v;
+        }
+      }
+    }
+    sa[W - 1] = ra[W - 1];
+    if constexpr (GRAD) sb[W - 1] = rb[W - 1];
+#pragma unroll
+    for (int i = W - 2; i >= 0; --i) {
+      sa[i] = wop<T, SUPA>(sa[i + 1], ra[i]);
+      if constexpr (GRAD) sb[i] = wop<T, false>(sb[i + 1], rb[i]);
+    }
+  }
+}
+
+template <typename T, bool SUP, int KY, int KX, bool GRAD>
 __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_constant__ CUtensorMap tmap,
                                                           uint32_t *__restrict__ out, int H, int Wn) {
-  using G = RectGeom<T, KY, KX>;
-  constexpr int E = G::E, HW = G::HW, BW = G::BW, TR = G::TR, TH = G::TH, TW = G::TW, THG = G::THG;
+  using G = RectGeom<T, KY, KX, GRAD>;
+  constexpr int E = G::E, HW = G::HW, BW = G::BW, TR = G::TR, TH = G::TH, TW = G::TW, THG = G::THG, MP = G::MP;
   using O = Op<T, SUP>;
   extern __shared__ __align__(128) uint32_t s_tile[];
   __shared__ int s_ok;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(s_tile + TR * BW);
+  uint32_t *s_min = s_tile + TR * BW;  // GRAD with a row pass: X-eroded centre words, [TR][MP]
+  uint64_t *bar = reinterpret_cast<uint64_t *>(s_tile + TR * BW + TR * MP);
   const unsigned bar_a = smem_u32(bar);
   const int t = threadIdx.x;
   const int wx0 = blockIdx.x * TW;         // first centre word
@@ -118,65 +254,41 @@ __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_consta
   if (!s_ok) return;
   (void)mbar_try(bar_a, 0);  // the phase is complete: each thread observes it (acquire)
 
-  // pixels outside the image (TMA fills them with zeros) become neutral
+  // pixels outside the image (TMA fills them with zeros): the neutral value of the operator, or for
+  // the gradient (two operators) the nearest image pixel -- a clipped box window always contains
+  // that pixel, so repeating it changes neither the maximum nor the minimum
   if (tx < 0 || ty < 0 || tx + BW > Wn || ty + TR > H) {
-    const uint32_t NEUW = splat<T>(O::neutral());
-    for (int r = 0; r < TR; ++r) {
-      const bool row_out = ty + r < 0 || ty + r >= H;
-      for (int c = t; c < BW; c += kRThreads)
-        if (row_out || tx + c < 0 || tx + c >= Wn) s_tile[r * BW + c] = NEUW;
+    if constexpr (!GRAD) {
+      const uint32_t NEUW = splat<T>(O::neutral());
+      for (int r = 0; r < TR; ++r) {
+        const bool row_out = ty + r < 0 || ty + r >= H;
+        for (int c = t; c < BW; c += kRThreads)
+          if (row_out || tx + c < 0 || tx + c >= Wn) s_tile[r * BW + c] = NEUW;
+      }
+    } else {
+      for (int r = 0; r < TR; ++r) {
+        if (ty + r < 0 || ty + r >= H) continue;
+        const uint32_t lw = splat<T>(px_of<T>(s_tile[r * BW + max(-tx, 0)], 0));
+        const uint32_t rw = splat<T>(px_of<T>(s_tile[r * BW + min(Wn - 1 - tx, BW - 1)], E - 1));
+        for (int c = t; c < BW; c += kRThreads) {
+          if (tx + c < 0) s_tile[r * BW + c] = lw;
+          else if (tx + c >= Wn) s_tile[r * BW + c] = rw;
+        }
+      }
+      __syncthreads();
+      for (int r = 0; r < TR; ++r) {
+        const int yr = ty + r;
+        if (yr >= 0 && yr < H) continue;
+        const int src = (yr < 0 ? 0 : H - 1) - ty;
+        for (int c = t; c < BW; c += kRThreads) s_tile[r * BW + c] = s_tile[src * BW + c];
+      }
     }
     __syncthreads();
   }
 
-  // ---- row pass: thread t scans input row t; stream pixel q is tile pixel P0 + q, output pixel j
-  // (tile pixel HW*E + j) is formed at q = j + 2KX
+  // ---- row pass: thread t scans input row t
   if constexpr (KX > 0) {
-    constexpr int K = KX, W = 2 * K + 1;
-    uint32_t *row = s_tile + t * BW;
-    constexpr int NQ = TW * E + 2 * K;
-    constexpr int NB = (NQ + W - 1) / W;
-    constexpr int P0 = HW * E - K;
-    constexpr int CH = 4 * E;  // pixels per 16-byte chunk
-    T suf[W];
-#pragma unroll
-    for (int i = 0; i < W; ++i) suf[i] = O::neutral();
-    uint32_t cw[4] = {0, 0, 0, 0}, acc[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-      T raw[W];
-#pragma unroll
-      for (int i = 0; i < W; ++i) {
-        const int q = b * W + i;
-        if (q < NQ) {
-          const int p = P0 + q;
-          if (q == 0 || p % CH == 0) {
-            const uint4 v = *reinterpret_cast<const uint4 *>(row + (p / CH) * 4);
-            cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
-          }
-          raw[i] = px_of<T>(cw[(p / E) % 4], p % E);
-        } else {
-          raw[i] = O::neutral();
-        }
-      }
-      T pre = raw[0];
-#pragma unroll
-      for (int i = 0; i < W; ++i) {
-        if (i > 0) pre = O::apply(pre, raw[i]);
-        const int j = b * W + i - 2 * K;
-        if (j >= 0 && j < TW * E) {
-          const T r = (i < W - 1) ? O::apply(suf[i + 1], pre) : pre;
-          const uint32_t v = bits_of<T>(r);
-          if (j % E == 0) acc[(j / E) % 4] = v;
-          else acc[(j / E) % 4] |= v << (8 * (int)sizeof(T) * (j % E));
-          if (j % CH == CH - 1)
-            *reinterpret_cast<uint4 *>(row + HW + (j / CH) * 4) = make_uint4(acc[0], acc[1], acc[2], acc[3]);
-        }
-      }
-      suf[W - 1] = raw[W - 1];
-#pragma unroll
-      for (int i = W - 2; i >= 0; --i) suf[i] = O::apply(suf[i + 1], raw[i]);
-    }
+    row_scan<T, SUP, KX, TW, HW, GRAD>(s_tile + t * BW, s_min + t * MP);
     __syncthreads();
   }
 
@@ -185,40 +297,19 @@ __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_consta
   // a vertical extent the centre words are copied out.
   const int j0 = (t / TW) * THG;
   const uint32_t *col = s_tile + j0 * BW + HW + t % TW;
+  constexpr int SB = KX > 0 ? MP : BW;
+  const uint32_t *colb = (GRAD && KX > 0) ? s_min + j0 * MP + t % TW : col;
   const int gx = wx0 + t % TW;
   if constexpr (KY == 0) {
     if (gx < Wn)
 #pragma unroll 4
-      for (int j = 0; j < THG && j0 + j < TH && y0 + j0 + j < H; ++j) out[(size_t)(y0 + j0 + j) * Wn + gx] = col[j * BW];
+      for (int j = 0; j < THG && j0 + j < TH && y0 + j0 + j < H; ++j) {
+        uint32_t v = col[j * BW];
+        if constexpr (GRAD) v = wdiff<T>(v, colb[j * SB]);
+        out[(size_t)(y0 + j0 + j) * Wn + gx] = v;
+      }
   } else {
-    constexpr int K = KY, W = 2 * K + 1;
-    const uint32_t NEUW = splat<T>(O::neutral());
-    constexpr int NB = (THG + 2 * K + W - 1) / W;
-    uint32_t suf[W];
-#pragma unroll
-    for (int i = 0; i < W; ++i) suf[i] = NEUW;
-#pragma unroll
-    for (int b = 0; b < NB; ++b) {
-      uint32_t raw[W];
-#pragma unroll
-      for (int i = 0; i < W; ++i) {
-        const int q = b * W + i;
-        raw[i] = (q < THG + 2 * K && j0 + q < TR) ? col[q * BW] : NEUW;
-      }
-      uint32_t pre = raw[0];
-#pragma unroll
-      for (int i = 0; i < W; ++i) {
-        if (i > 0) pre = wop<T, SUP>(pre, raw[i]);
-        const int j = b * W + i - 2 * K;
-        if (j >= 0 && j < THG && j0 + j < TH) {
-          const int gy = y0 + j0 + j;
-          if (gy < H && gx < Wn) out[(size_t)gy * Wn + gx] = (i < W - 1) ? wop<T, SUP>(suf[i + 1], pre) : pre;
-        }
-      }
-      suf[W - 1] = raw[W - 1];
-#pragma unroll
-      for (int i = W - 2; i >= 0; --i) suf[i] = wop<T, SUP>(suf[i + 1], raw[i]);
-    }
+    col_scan<T, SUP, KY, THG, TH, TR, BW, SB, GRAD>(col, colb, out, j0, y0, gx, H, Wn);
   }
 }
 
@@ -237,9 +328,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
   return fn;
 }
 
-template <typename T, bool SUP, int KY, int KX>
+template <typename T, bool SUP, int KY, int KX, bool GRAD>
 pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
-  using G = RectGeom<T, KY, KX>;
+  using G = RectGeom<T, KY, KX, GRAD>;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, Wn = d.nx / G::E;
   auto fn = encode_tiled();
@@ -259,13 +350,14 @@ pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
   PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
   const uint64_t bit = 1ull << (dev & 63);
   if (!(attr_devices.load() & bit)) {
-    PG_CUDA_TRY(cudaFuncSetAttribute(k_rect_fused<T, SUP, KY, KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    PG_CUDA_TRY(cudaFuncSetAttribute(k_rect_fused<T, SUP, KY, KX, GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)G::smem),
                 "tile kernel smem attribute");
     attr_devices.fetch_or(bit);
   }
   const dim3 grid((unsigned)ceil_div(Wn, G::TW), (unsigned)ceil_div(H, G::TH));
-  k_rect_fused<T, SUP, KY, KX><<<grid, kRThreads, G::smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H, (int)Wn);
+  k_rect_fused<T, SUP, KY, KX, GRAD><<<grid, kRThreads, G::smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H,
+                                                                     (int)Wn);
   return cuda_status(cudaGetLastError(), "tile erosion / dilation launch");
 }
 
@@ -274,31 +366,49 @@ template <typename T, bool SUP>
 pg_status rect_fused_k(const pg_image &in, const pg_image &out, int hy, int hx, cudaStream_t s) {
   if (hy == hx) {
     switch (hy) {
-      case 7: return rect_fused<T, SUP, 7, 7>(in, out, s);
-      case 15: return rect_fused<T, SUP, 15, 15>(in, out, s);
-      default: return rect_fused<T, SUP, 31, 31>(in, out, s);
+      case 7: return rect_fused<T, SUP, 7, 7, false>(in, out, s);
+      case 15: return rect_fused<T, SUP, 15, 15, false>(in, out, s);
+      default: return rect_fused<T, SUP, 31, 31, false>(in, out, s);
     }
   }
   if (hy == 0) {
     switch (hx) {
-      case 7: return rect_fused<T, SUP, 0, 7>(in, out, s);
-      case 15: return rect_fused<T, SUP, 0, 15>(in, out, s);
-      default: return rect_fused<T, SUP, 0, 31>(in, out, s);
+      case 7: return rect_fused<T, SUP, 0, 7, false>(in, out, s);
+      case 15: return rect_fused<T, SUP, 0, 15, false>(in, out, s);
+      default: return rect_fused<T, SUP, 0, 31, false>(in, out, s);
     }
   }
   switch (hy) {
-    case 7: return rect_fused<T, SUP, 7, 0>(in, out, s);
-    case 15: return rect_fused<T, SUP, 15, 0>(in, out, s);
-    default: return rect_fused<T, SUP, 31, 0>(in, out, s);
+    case 7: return rect_fused<T, SUP, 7, 0, false>(in, out, s);
+    case 15: return rect_fused<T, SUP, 15, 0, false>(in, out, s);
+    default: return rect_fused<T, SUP, 31, 0, false>(in, out, s);
+  }
+}
+
+// the gradient (dilation - erosion) in one pass; not for the 63 x 63 square
+template <typename T>
+pg_status rect_grad_k(const pg_image &in, const pg_image &out, int hy, int hx, cudaStream_t s) {
+  if (hy == hx) return hy == 7 ? rect_fused<T, true, 7, 7, true>(in, out, s) : rect_fused<T, true, 15, 15, true>(in, out, s);
+  if (hy == 0) {
+    switch (hx) {
+      case 7: return rect_fused<T, true, 0, 7, true>(in, out, s);
+      case 15: return rect_fused<T, true, 0, 15, true>(in, out, s);
+      default: return rect_fused<T, true, 0, 31, true>(in, out, s);
+    }
+  }
+  switch (hy) {
+    case 7: return rect_fused<T, true, 7, 0, true>(in, out, s);
+    case 15: return rect_fused<T, true, 15, 0, true>(in, out, s);
+    default: return rect_fused<T, true, 31, 0, true>(in, out, s);
   }
 }
 
 }  // namespace
 
-bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
-                    pg_status *st) {
+bool rect_fused_ok(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool grad) {
   auto ok_k = [](int64_t k) { return k == 7 || k == 15 || k == 31; };
   if (in.rank != 2 || !((hy == hx && ok_k(hy)) || (hy == 0 && ok_k(hx)) || (hx == 0 && ok_k(hy)))) return false;
+  if (grad && hy == 31 && hx == 31) return false;
   const int es = elem_size(in.ptype);
   // 2- and 4-byte pixels (for u8 the row pass's register window spills; the two line passes run)
   if (es != 2 && es != 4) return false;
@@ -307,6 +417,12 @@ bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t
   if (H < 1 || Wd < 1 || (Wd * es) % 16 != 0) return false;
   if ((reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 16 != 0) return false;
   if (H > (1 << 30) || Wd * es / 4 > (1 << 30) || ceil_div(H, kRThreads - 2 * hy) > 65535) return false;
+  return in.ptype == PG_PTYPE_U16 || in.ptype == PG_PTYPE_I32 || in.ptype == PG_PTYPE_F32;
+}
+
+bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
+                    pg_status *st) {
+  if (!rect_fused_ok(in, out, hy, hx, false)) return false;
   const int y = (int)hy, x = (int)hx;
   switch (in.ptype) {
     case PG_PTYPE_U16:
@@ -318,6 +434,17 @@ bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t
     case PG_PTYPE_F32:
       *st = dilate ? rect_fused_k<float, true>(in, out, y, x, s) : rect_fused_k<float, false>(in, out, y, x, s);
       return true;
+    default: return false;
+  }
+}
+
+bool try_rect_gradient(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, cudaStream_t s, pg_status *st) {
+  if (!rect_fused_ok(in, out, hy, hx, true)) return false;
+  const int y = (int)hy, x = (int)hx;
+  switch (in.ptype) {
+    case PG_PTYPE_U16: *st = rect_grad_k<uint16_t>(in, out, y, x, s); return true;
+    case PG_PTYPE_I32: *st = rect_grad_k<int32_t>(in, out, y, x, s); return true;
+    case PG_PTYPE_F32: *st = rect_grad_k<float>(in, out, y, x, s); return true;
     default: return false;
   }
 }
