@@ -274,6 +274,8 @@ static pg_status composite(const pg_image &in, const pg_se &se, const pg_image &
   pg_status st = PG_OK;
   // the gradient of a box: dilation and erosion of one tile in one pass (rect.cu)
   if (c == C_GRAD && se_box(se, in.rank, hy, hx) && try_rect_gradient(in, out, hy, hx, s, &st)) return st;
+  // opening / closing of a box: both operators on one tile (rect_open.cu)
+  if (c != C_GRAD && se_box(se, in.rank, hy, hx) && try_rect_open(in, out, hy, hx, c == C_OPEN, s, &st)) return st;
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
   pg_image t = in;

@@ -198,6 +198,10 @@ bool rect_fused_ok(const pg_image &in, const pg_image &out, int64_t hy, int64_t 
 bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
                     pg_status *st);
 bool try_rect_gradient(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, cudaStream_t s, pg_status *st);
+// One-pass opening / closing by an X segment (rect_open.cu): hy = 0, hx = 7, 15, 31.
+bool try_rect_open(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool opening, cudaStream_t s,
+                   pg_status *st);
+int take_open_status();  // device status of the one-pass opening kernel since the last call (0: none)
 int take_rect_status();  // device status of the fused square kernel since the last call (0: none)
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);

@@ -1605,7 +1605,9 @@ pg_status pg_check_device(pg_stream_t stream) {
     return pg::fail(static_cast<pg_status>(st), "reconstruction did not converge within its round cap or wait limit");
   }
   if (const int rs = pg::take_rect_status())
-    return pg::fail(static_cast<pg_status>(rs), "a square tile load did not complete within its wait limit");
+    return pg::fail(static_cast<pg_status>(rs), "a box tile load did not complete within its wait limit");
+  if (const int os = pg::take_open_status())
+    return pg::fail(static_cast<pg_status>(os), "an opening tile load did not complete within its wait limit");
   return PG_OK;
 }
 

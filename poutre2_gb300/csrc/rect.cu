@@ -24,16 +24,11 @@
 // image.  Pixels outside the image then repeat the nearest image pixel instead of a neutral value (a
 // clipped box window contains that pixel, so neither extremum changes).
 //
-// The wait on the mbarrier is bounded (kRectWaitNs of %globaltimer); on expiry the CTA records
+// The wait on the mbarrier is bounded (tile::kWaitNs of %globaltimer); on expiry the CTA records
 // PG_ERR_CUDA in g_rect_status (read by pg_check_device) and leaves its tile unwritten.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include <atomic>
-#include <mutex>
 
-#include "common.cuh"
-#include "words.cuh"
+#include "tile.cuh"
 
 namespace pg {
 
@@ -41,8 +36,8 @@ __device__ int g_rect_status = 0;
 
 namespace {
 
-constexpr int kRThreads = 128;                             // = input rows per tile
-constexpr unsigned long long kRectWaitNs = 1000000000ull;  // 1 s
+using namespace tile;
+constexpr int kRThreads = tile::kThreads;
 
 template <typename T, int KY, int KX, bool GRAD> struct RectGeom {
   static constexpr int E = 4 / (int)sizeof(T);
@@ -64,160 +59,6 @@ template <typename T, int KY, int KX, bool GRAD> struct RectGeom {
   static_assert(!GRAD || !(KY > 15 && KX > 0), "gradient: register window too large");
 };
 
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ unsigned long long now_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-template <typename T> __device__ __forceinline__ T px_of(uint32_t w, int k) {
-  if constexpr (std::is_same_v<T, float>) return __uint_as_float(w);
-  else if constexpr (sizeof(T) == 4) return (T)w;
-  else return (T)(w >> (8 * (int)sizeof(T) * k));
-}
-// a - b per pixel of a word, where a >= b in every pixel (a dilation minus an erosion): packed
-// unsigned pixels never borrow from the next lane, so one 32-bit subtraction is exact; i32 wraps like
-// the difference kernel's int arithmetic; f32 is one rounded subtraction, as there
-template <typename T> __device__ __forceinline__ uint32_t wdiff(uint32_t a, uint32_t b) {
-  if constexpr (std::is_same_v<T, float>) return __float_as_uint(__uint_as_float(a) - __uint_as_float(b));
-  else return a - b;
-}
-template <typename T> __device__ __forceinline__ uint32_t bits_of(T v) {
-  if constexpr (std::is_same_v<T, float>) return __float_as_uint(v);
-  else return (uint32_t)v;
-}
-
-// Row scan of one tile row (registers), in place: stream pixel q is tile pixel P0 + q, output
-// pixel j (tile pixel HW*E + j) is formed at q = j + 2K.  With GRAD both the dilation (in place) and
-// the erosion (into `mrow`) are formed from the same pixels.
-template <typename T, bool SUP, int K, int TW, int HW, bool GRAD>
-__device__ __forceinline__ void row_scan(uint32_t *row, uint32_t *mrow) {
-  constexpr int E = 4 / (int)sizeof(T), W = 2 * K + 1;
-  constexpr int NQ = TW * E + 2 * K, NB = (NQ + W - 1) / W, P0 = HW * E - K;
-  constexpr int CH = 4 * E;  // pixels per 16-byte chunk
-  using A = Op<T, GRAD ? true : SUP>;
-  using B = Op<T, false>;
-  T sa[W], sb[GRAD ? W : 1];
-#pragma unroll
-  for (int i = 0; i < W; ++i) {
-    sa[i] = A::neutral();
-    if constexpr (GRAD) sb[i] = B::neutral();
-  }
-  uint32_t cw[4] = {0, 0, 0, 0}, acca[4] = {0, 0, 0, 0}, accb[4] = {0, 0, 0, 0};
-#pragma unroll
-  for (int b = 0; b < NB; ++b) {
-    T raw[W];
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      const int q = b * W + i;
-      if (q < NQ) {
-        const int p = P0 + q;
-        if (q == 0 || p % CH == 0) {
-          const uint4 v = *reinterpret_cast<const uint4 *>(row + (p / CH) * 4);
-          cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
-        }
-        raw[i] = px_of<T>(cw[(p / E) % 4], p % E);
-      } else {
-        raw[i] = A::neutral();  // beyond the stream: feeds no output
-      }
-    }
-    T pa = raw[0], pb = raw[0];
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      if (i > 0) {
-        pa = A::apply(pa, raw[i]);
-        if constexpr (GRAD) pb = B::apply(pb, raw[i]);
-      }
-      const int j = b * W + i - 2 * K;
-      if (j >= 0 && j < TW * E) {
-        const int sh = 8 * (int)sizeof(T) * (j % E), wi = (j / E) % 4;
-        const uint32_t va = bits_of<T>((i < W - 1) ? A::apply(sa[i + 1], pa) : pa);
-        acca[wi] = (j % E == 0) ? va : (acca[wi] | (va << sh));
-        if constexpr (GRAD) {
-          const uint32_t vb = bits_of<T>((i < W - 1) ? B::apply(sb[i + 1], pb) : pb);
-          accb[wi] = (j % E == 0) ? vb : (accb[wi] | (vb << sh));
-        }
-        if (j % CH == CH - 1) {
-          *reinterpret_cast<uint4 *>(row + HW + (j / CH) * 4) = make_uint4(acca[0], acca[1], acca[2], acca[3]);
-          if constexpr (GRAD)
-            *reinterpret_cast<uint4 *>(mrow + (j / CH) * 4) = make_uint4(accb[0], accb[1], accb[2], accb[3]);
-        }
-      }
-    }
-    sa[W - 1] = raw[W - 1];
-    if constexpr (GRAD) sb[W - 1] = raw[W - 1];
-#pragma unroll
-    for (int i = W - 2; i >= 0; --i) {
-      sa[i] = A::apply(sa[i + 1], raw[i]);
-      if constexpr (GRAD) sb[i] = B::apply(sb[i + 1], raw[i]);
-    }
-  }
-}
-
-// Column scan of THG output rows (registers) from words `ca` (stride SA) -- and, with GRAD, the
-// erosion from `cb` (stride SB) -- written to out[row y0 + j0 + j][gx] (GRAD: dilation - erosion).
-template <typename T, bool SUP, int K, int THG, int TH, int TR, int SA, int SB, bool GRAD>
-__device__ __forceinline__ void col_scan(const uint32_t *ca, const uint32_t *cb, uint32_t *__restrict__ out,
-                                         int j0, int y0, int gx, int H, int Wn) {
-  constexpr int W = 2 * K + 1, NB = (THG + 2 * K + W - 1) / W;
-  constexpr bool SUPA = GRAD ? true : SUP;
-  const uint32_t NA = splat<T>(Op<T, SUPA>::neutral()), NBW = splat<T>(Op<T, false>::neutral());
-  uint32_t sa[W], sb[GRAD ? W : 1];
-#pragma unroll
-  for (int i = 0; i < W; ++i) {
-    sa[i] = NA;
-    if constexpr (GRAD) sb[i] = NBW;
-  }
-#pragma unroll
-  for (int b = 0; b < NB; ++b) {
-    uint32_t ra[W], rb[GRAD ? W : 1];
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      const int q = b * W + i;
-      const bool in = q < THG + 2 * K && j0 + q < TR;
-      ra[i] = in ? ca[q * SA] : NA;
-      if constexpr (GRAD) rb[i] = in ? cb[q * SB] : NBW;
-    }
-    uint32_t pa = ra[0], pb = 0u;
-    if constexpr (GRAD) pb = rb[0];
-#pragma unroll
-    for (int i = 0; i < W; ++i) {
-      if (i > 0) {
-        pa = wop<T, SUPA>(pa, ra[i]);
-        if constexpr (GRAD) pb = wop<T, false>(pb, rb[i]);
-      }
-      const int j = b * W + i - 2 * K;
-      if (j >= 0 && j < THG && j0 + j < TH) {
-        const int gy = y0 + j0 + j;
-        if (gy < H && gx < Wn) {
-          uint32_t v = (i < W - 1) ? wop<T, SUPA>(sa[i + 1], pa) : pa;
-          if constexpr (GRAD) v = wdiff<T>(v, (i < W - 1) ? wop<T, false>(sb[i + 1], pb) : pb);
-          out[(size_t)gy * Wn + gx] = v;
-        }
-      }
-    }
-    sa[W - 1] = ra[W - 1];
-    if constexpr (GRAD) sb[W - 1] = rb[W - 1];
-#pragma unroll
-    for (int i = W - 2; i >= 0; --i) {
-      sa[i] = wop<T, SUPA>(sa[i + 1], ra[i]);
-      if constexpr (GRAD) sb[i] = wop<T, false>(sb[i + 1], rb[i]);
-    }
-  }
-}
-
 template <typename T, bool SUP, int KY, int KX, bool GRAD>
 __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_constant__ CUtensorMap tmap,
                                                           uint32_t *__restrict__ out, int H, int Wn) {
@@ -228,31 +69,12 @@ __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_consta
   __shared__ int s_ok;
   uint32_t *s_min = s_tile + TR * BW;  // GRAD with a row pass: X-eroded centre words, [TR][MP]
   uint64_t *bar = reinterpret_cast<uint64_t *>(s_tile + TR * BW + TR * MP);
-  const unsigned bar_a = smem_u32(bar);
   const int t = threadIdx.x;
   const int wx0 = blockIdx.x * TW;         // first centre word
   const int y0 = blockIdx.y * TH;          // first output row
   const int tx = wx0 - HW, ty = y0 - KY;   // tile origin: word (a multiple of 4), row
 
-  if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"((unsigned)G::tile_bytes)
-                 : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(s_tile)),
-        "l"(&tmap), "r"(tx), "r"(ty), "r"(bar_a)
-        : "memory");
-    bool done = mbar_try(bar_a, 0);
-    const unsigned long long t0 = now_ns();
-    while (!done && now_ns() - t0 < kRectWaitNs) done = mbar_try(bar_a, 0);
-    if (!done) atomicCAS(&g_rect_status, 0, (int)PG_ERR_CUDA);
-    s_ok = done;
-  }
-  __syncthreads();
-  if (!s_ok) return;
-  (void)mbar_try(bar_a, 0);  // the phase is complete: each thread observes it (acquire)
+  if (!load_tile(&tmap, s_tile, bar, (unsigned)G::tile_bytes, tx, ty, &g_rect_status, &s_ok)) return;
 
   // pixels outside the image (TMA fills them with zeros): the neutral value of the operator, or for
   // the gradient (two operators) the nearest image pixel -- a clipped box window always contains
@@ -313,37 +135,13 @@ __global__ void __launch_bounds__(kRThreads, 1) k_rect_fused(const __grid_consta
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      (void)cudaGetLastError();
-  });
-  return fn;
-}
-
 template <typename T, bool SUP, int KY, int KX, bool GRAD>
 pg_status rect_fused(const pg_image &in, const pg_image &out, cudaStream_t s) {
   using G = RectGeom<T, KY, KX, GRAD>;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, Wn = d.nx / G::E;
-  auto fn = encode_tiled();
-  if (!fn) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   CUtensorMap map;
-  cuuint64_t dims[2] = {(cuuint64_t)Wn, (cuuint64_t)H};
-  cuuint64_t strides[1] = {(cuuint64_t)Wn * 4};
-  cuuint32_t box[2] = {(cuuint32_t)G::BW, (cuuint32_t)G::TR};
-  cuuint32_t estr[2] = {1, 1};
-  const CUresult r = fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, in.data, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the rectangle tile");
+  PG_TRY(word_map(&map, in.data, H, Wn, G::BW, G::TR));
   // the opt-in shared-memory size is a per-device attribute of each instantiation
   static std::atomic<uint64_t> attr_devices{0};
   int dev = 0;

@@ -245,6 +245,10 @@ def test_square_one_pass(dt, k, form):
         out = torch.empty_like(x)
         llm.Gradient(x, llm.se_rect(hy, hx), out)
         np.testing.assert_array_equal(host(out), (d - e).astype(a.dtype), err_msg=f"{shape} gradient")
+        for fn, exp in ((llm.Opening, oracle.rect(e, hy, hx, True)), (llm.Closing, oracle.rect(d, hy, hx, False))):
+            out = torch.empty_like(x)
+            fn(x, llm.se_rect(hy, hx), out)
+            np.testing.assert_array_equal(host(out), exp, err_msg=f"{shape} {fn.__name__}")
     import ctypes
     from poutre2_gb300 import _lib
     _lib.call("pg_check_device", ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))  # raises on a device error
