@@ -241,8 +241,8 @@ PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker,
 
 /* Synchronises `stream`, then returns (and clears) the device-side status of the kernels:
  * PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device wait), or
- * PG_ERR_CUDA when a one-pass square erosion / dilation found a tile load unfinished after its
- * bounded wait, since the last check; else PG_OK.  The calls are asynchronous; call this to
+ * PG_ERR_CUDA when a shared-memory tile kernel (box erosion / dilation, gradient, opening) found a
+ * tile load unfinished after its bounded wait, since the last check; else PG_OK.  The calls are asynchronous; call this to
  * observe the failure the reference would have thrown. */
 PG_API pg_status pg_check_device(pg_stream_t stream);
 
