@@ -128,7 +128,9 @@ def test_static_3d(dt, se):
     from poutre2_gb300 import llm
     from poutre2_gb300.se import Common_NL_SE
     rng = np.random.default_rng(5)
-    for shape in [(1, 1, 1), (3, 3, 3), (5, 7, 9), (17, 20, 64), (2, 33, 31)]:
+    # rows of a multiple of 16 bytes take the slice-streaming cube kernel: one slice, several tiles
+    # across, down and in depth
+    for shape in [(1, 1, 1), (3, 3, 3), (5, 7, 9), (17, 20, 64), (2, 33, 31), (1, 5, 16), (19, 70, 160), (9, 40, 528)]:
         a = rand(rng, shape, dt)
         x = dev(a)
         for dil in (True, False):
