@@ -173,12 +173,16 @@ __device__ __forceinline__ void col_scan(const uint32_t *ca, const uint32_t *cb,
 
 
 // TMA copy of the box at word tx, row ty into s (bytes long), completing on the mbarrier `bar`;
-// thread 0 waits at most kWaitNs and records PG_ERR_CUDA in *status on expiry.  Returns, for every
+// thread 0 waits at most kWaitNs and records PG_ERR_CUDA in *status on expiry (and refuses to copy
+// into an s that is not 128-byte aligned).  Returns, for every
 // thread of the CTA, whether the tile arrived (one __syncthreads inside).
 __device__ __forceinline__ bool load_tile(const CUtensorMap *map, uint32_t *s, uint64_t *bar, unsigned bytes, int tx,
                                           int ty, int *status, int *s_ok) {
   const unsigned bar_a = smem_u32(bar);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && (smem_u32(s) & 127u)) {  // a TMA destination starts on a 128-byte boundary
+    atomicCAS(status, 0, (int)PG_ERR_CUDA);
+    *s_ok = 0;
+  } else if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(bytes) : "memory");
