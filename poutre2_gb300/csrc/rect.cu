@@ -1,5 +1,6 @@
 // rect.cu -- erosion / dilation by the (2KY+1) x (2KX+1) box in one pass through shared memory: the
-// square (KY = KX), the X segment (KY = 0) and the Y segment (KX = 0), for K = 7, 15, 31.
+// square (KY = KX), the X segment (KY = 0) and the Y segment (KX = 0), for K = 7, 15, 31; 2- and 4-byte
+// pixels, and 1-byte pixels for the Y segment.
 //
 // Same result as the separable line passes of line.cu (DilateX then DilateY over a clipped window;
 // the box is the Minkowski sum of an X and a Y segment, so the order is immaterial): one tile is read
@@ -208,14 +209,25 @@ bool rect_fused_ok(const pg_image &in, const pg_image &out, int64_t hy, int64_t 
   if (in.rank != 2 || !((hy == hx && ok_k(hy)) || (hy == 0 && ok_k(hx)) || (hx == 0 && ok_k(hy)))) return false;
   if (grad && hy == 31 && hx == 31) return false;
   const int es = elem_size(in.ptype);
-  // 2- and 4-byte pixels (for u8 the row pass's register window spills; the two line passes run)
-  if (es != 2 && es != 4) return false;
+  // 2- and 4-byte pixels; u8 only without a row pass (its register window of single pixels spills:
+  // the line passes run instead)
+  if (es != 2 && es != 4 && !(es == 1 && hx == 0)) return false;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, Wd = d.nx;
   if (H < 1 || Wd < 1 || (Wd * es) % 16 != 0) return false;
   if ((reinterpret_cast<uintptr_t>(in.data) | reinterpret_cast<uintptr_t>(out.data)) % 16 != 0) return false;
   if (H > (1 << 30) || Wd * es / 4 > (1 << 30) || ceil_div(H, kRThreads - 2 * hy) > 65535) return false;
-  return in.ptype == PG_PTYPE_U16 || in.ptype == PG_PTYPE_I32 || in.ptype == PG_PTYPE_F32;
+  return in.ptype == PG_PTYPE_U8 || in.ptype == PG_PTYPE_U16 || in.ptype == PG_PTYPE_I32 || in.ptype == PG_PTYPE_F32;
+}
+
+// u8: Y segments only (no row pass)
+template <bool SUP, bool GRAD>
+pg_status rect_fused_u8_y(const pg_image &in, const pg_image &out, int hy, cudaStream_t s) {
+  switch (hy) {
+    case 7: return rect_fused<uint8_t, SUP, 7, 0, GRAD>(in, out, s);
+    case 15: return rect_fused<uint8_t, SUP, 15, 0, GRAD>(in, out, s);
+    default: return rect_fused<uint8_t, SUP, 31, 0, GRAD>(in, out, s);
+  }
 }
 
 bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s,
@@ -223,6 +235,9 @@ bool try_rect_fused(const pg_image &in, const pg_image &out, int64_t hy, int64_t
   if (!rect_fused_ok(in, out, hy, hx, false)) return false;
   const int y = (int)hy, x = (int)hx;
   switch (in.ptype) {
+    case PG_PTYPE_U8:
+      *st = dilate ? rect_fused_u8_y<true, false>(in, out, y, s) : rect_fused_u8_y<false, false>(in, out, y, s);
+      return true;
     case PG_PTYPE_U16:
       *st = dilate ? rect_fused_k<uint16_t, true>(in, out, y, x, s) : rect_fused_k<uint16_t, false>(in, out, y, x, s);
       return true;
@@ -240,6 +255,7 @@ bool try_rect_gradient(const pg_image &in, const pg_image &out, int64_t hy, int6
   if (!rect_fused_ok(in, out, hy, hx, true)) return false;
   const int y = (int)hy, x = (int)hx;
   switch (in.ptype) {
+    case PG_PTYPE_U8: *st = rect_fused_u8_y<true, true>(in, out, y, s); return true;
     case PG_PTYPE_U16: *st = rect_grad_k<uint16_t>(in, out, y, x, s); return true;
     case PG_PTYPE_I32: *st = rect_grad_k<int32_t>(in, out, y, x, s); return true;
     case PG_PTYPE_F32: *st = rect_grad_k<float>(in, out, y, x, s); return true;
