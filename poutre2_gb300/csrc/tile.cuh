@@ -55,8 +55,76 @@ template <typename T> __device__ __forceinline__ uint32_t bits_of(T v) {
 // Row scan of one tile row (registers), in place: stream pixel q is tile pixel P0 + q, output
 // pixel j (tile pixel HW*E + j) is formed at q = j + 2K.  With GRAD both the dilation (in place) and
 // the erosion (into `mrow`) are formed from the same pixels.
+// Row scan of 2-byte pixels kept in pairs (word m = pixels 2m, 2m + 1), K = 2k + 1 odd, NOUT output
+// words from word OUT0, in place.  With A(m) = op over words [m - k, m + k] and B(m) = op(A(m), word
+// m - k - 1), pixel 2m's window [2m - K, 2m + K] holds the even pixels of A(m) and the odd pixels of
+// B(m), and pixel 2m + 1's window the odd pixels of A(m) and the even pixels of B(m + 1), so
+//   out word m = op(A(m), (odd half of B(m), even half of B(m + 1))).
+// One van Herk / Gil-Werman scan over words (window 2k + 1) gives A; the word k + 1 left of A(m)'s
+// window is the same register of the previous block.  Output word m - 1 is formed with A(m).
+template <bool SUP, int K, int NOUT, int OUT0>
+__device__ __forceinline__ void row_scan_pairs(uint32_t *row) {
+  using T = uint16_t;
+  constexpr int k = (K - 1) / 2, W = 2 * k + 1;
+  constexpr int Q0 = OUT0 - k - 1;          // stream word 0 (a multiple of 4)
+  constexpr int NQ = NOUT + 2 * k + 2;      // words Q0 .. OUT0 + NOUT + k
+  constexpr int NB = (NQ + W - 1) / W;
+  static_assert(K % 2 == 1 && Q0 >= 0 && Q0 % 4 == 0 && OUT0 % 4 == 0 && NOUT % 4 == 0, "pair scan geometry");
+  const uint32_t NEUW = splat<T>(Op<T, SUP>::neutral());
+  uint32_t suf[W], prev[W];
+#pragma unroll
+  for (int i = 0; i < W; ++i) suf[i] = prev[i] = NEUW;
+  uint32_t cw[4] = {0, 0, 0, 0}, acc[4] = {0, 0, 0, 0};
+  uint32_t a_last = NEUW, b_last = NEUW;  // A(m - 1), B(m - 1)
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    uint32_t raw[W];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      const int s = b * W + i;
+      if (s < NQ) {
+        const int q = Q0 + s;
+        if (q % 4 == 0) {
+          const uint4 v = *reinterpret_cast<const uint4 *>(row + q);
+          cw[0] = v.x; cw[1] = v.y; cw[2] = v.z; cw[3] = v.w;
+        }
+        raw[i] = cw[q % 4];
+      } else {
+        raw[i] = NEUW;
+      }
+    }
+    uint32_t pre = raw[0];
+#pragma unroll
+    for (int i = 0; i < W; ++i) {
+      if (i > 0) pre = wop<T, SUP>(pre, raw[i]);
+      const int j = b * W + i - 2 * k;  // window start in the stream: A(m), m = Q0 + j + k
+      if (j >= 0) {
+        const uint32_t A = (i < W - 1) ? wop<T, SUP>(suf[i + 1], pre) : pre;
+        const uint32_t B = wop<T, SUP>(A, b > 0 ? prev[i] : NEUW);  // stream word j - 1 = one block back
+        const int mo = Q0 + j + k - 1 - OUT0;  // output word (from OUT0) formed now
+        if (mo >= 0 && mo < NOUT) {
+          acc[mo % 4] = wop<T, SUP>(a_last, __byte_perm(b_last, B, 0x5432));
+          if (mo % 4 == 3)
+            *reinterpret_cast<uint4 *>(row + OUT0 + mo - 3) = make_uint4(acc[0], acc[1], acc[2], acc[3]);
+        }
+        a_last = A;
+        b_last = B;
+      }
+    }
+    suf[W - 1] = raw[W - 1];
+#pragma unroll
+    for (int i = W - 2; i >= 0; --i) suf[i] = wop<T, SUP>(suf[i + 1], raw[i]);
+#pragma unroll
+    for (int i = 0; i < W; ++i) prev[i] = raw[i];
+  }
+}
+
 template <typename T, bool SUP, int K, int TW, int HW, bool GRAD>
 __device__ __forceinline__ void row_scan(uint32_t *row, uint32_t *mrow) {
+  if constexpr (sizeof(T) == 2 && !GRAD && K % 2 == 1 && HW - (K + 1) / 2 >= 0 && (HW - (K + 1) / 2) % 4 == 0) {
+    row_scan_pairs<SUP, K, TW, HW>(row);  // whole words, about half the operations per pixel
+    return;
+  }
   constexpr int E = 4 / (int)sizeof(T), W = 2 * K + 1;
   constexpr int NQ = TW * E + 2 * K, NB = (NQ + W - 1) / W, P0 = HW * E - K;
   constexpr int CH = 4 * E;  // pixels per 16-byte chunk
