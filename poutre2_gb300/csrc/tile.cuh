@@ -62,20 +62,25 @@ template <typename T> __device__ __forceinline__ uint32_t bits_of(T v) {
 //   out word m = op(A(m), (odd half of B(m), even half of B(m + 1))).
 // One van Herk / Gil-Werman scan over words (window 2k + 1) gives A; the word k + 1 left of A(m)'s
 // window is the same register of the previous block.  Output word m - 1 is formed with A(m).
-template <bool SUP, int K, int NOUT, int OUT0>
-__device__ __forceinline__ void row_scan_pairs(uint32_t *row) {
+template <bool SUP, int K, int NOUT, int OUT0, bool GRAD>
+__device__ __forceinline__ void row_scan_pairs(uint32_t *row, uint32_t *mrow) {
   using T = uint16_t;
+  constexpr bool SA = GRAD ? true : SUP;    // GRAD: dilation in place, erosion into mrow
   constexpr int k = (K - 1) / 2, W = 2 * k + 1;
   constexpr int Q0 = OUT0 - k - 1;          // stream word 0 (a multiple of 4)
   constexpr int NQ = NOUT + 2 * k + 2;      // words Q0 .. OUT0 + NOUT + k
   constexpr int NB = (NQ + W - 1) / W;
   static_assert(K % 2 == 1 && Q0 >= 0 && Q0 % 4 == 0 && OUT0 % 4 == 0 && NOUT % 4 == 0, "pair scan geometry");
-  const uint32_t NEUW = splat<T>(Op<T, SUP>::neutral());
-  uint32_t suf[W], prev[W];
+  const uint32_t NA = splat<T>(Op<T, SA>::neutral()), NBW = splat<T>(Op<T, false>::neutral());
+  uint32_t sa[W], sb[GRAD ? W : 1], prev[W];
 #pragma unroll
-  for (int i = 0; i < W; ++i) suf[i] = prev[i] = NEUW;
-  uint32_t cw[4] = {0, 0, 0, 0}, acc[4] = {0, 0, 0, 0};
-  uint32_t a_last = NEUW, b_last = NEUW;  // A(m - 1), B(m - 1)
+  for (int i = 0; i < W; ++i) {
+    sa[i] = NA;
+    prev[i] = NA;
+    if constexpr (GRAD) sb[i] = NBW;
+  }
+  uint32_t cw[4] = {0, 0, 0, 0}, acca[4] = {0, 0, 0, 0}, accb[4] = {0, 0, 0, 0};
+  uint32_t a_last = NA, b_last = NA, c_last = NBW, d_last = NBW;  // A(m - 1), B(m - 1) per operator
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
     uint32_t raw[W];
@@ -90,30 +95,45 @@ __device__ __forceinline__ void row_scan_pairs(uint32_t *row) {
         }
         raw[i] = cw[q % 4];
       } else {
-        raw[i] = NEUW;
+        raw[i] = NA;  // beyond the stream: feeds no output
       }
     }
-    uint32_t pre = raw[0];
+    uint32_t pa = raw[0], pb = raw[0];
 #pragma unroll
     for (int i = 0; i < W; ++i) {
-      if (i > 0) pre = wop<T, SUP>(pre, raw[i]);
+      if (i > 0) {
+        pa = wop<T, SA>(pa, raw[i]);
+        if constexpr (GRAD) pb = wop<T, false>(pb, raw[i]);
+      }
       const int j = b * W + i - 2 * k;  // window start in the stream: A(m), m = Q0 + j + k
       if (j >= 0) {
-        const uint32_t A = (i < W - 1) ? wop<T, SUP>(suf[i + 1], pre) : pre;
-        const uint32_t B = wop<T, SUP>(A, b > 0 ? prev[i] : NEUW);  // stream word j - 1 = one block back
         const int mo = Q0 + j + k - 1 - OUT0;  // output word (from OUT0) formed now
-        if (mo >= 0 && mo < NOUT) {
-          acc[mo % 4] = wop<T, SUP>(a_last, __byte_perm(b_last, B, 0x5432));
-          if (mo % 4 == 3)
-            *reinterpret_cast<uint4 *>(row + OUT0 + mo - 3) = make_uint4(acc[0], acc[1], acc[2], acc[3]);
-        }
+        const uint32_t A = (i < W - 1) ? wop<T, SA>(sa[i + 1], pa) : pa;
+        const uint32_t B = wop<T, SA>(A, b > 0 ? prev[i] : NA);  // stream word j - 1 = one block back
+        if (mo >= 0 && mo < NOUT) acca[mo % 4] = wop<T, SA>(a_last, __byte_perm(b_last, B, 0x5432));
         a_last = A;
         b_last = B;
+        if constexpr (GRAD) {
+          const uint32_t C = (i < W - 1) ? wop<T, false>(sb[i + 1], pb) : pb;
+          const uint32_t D = wop<T, false>(C, b > 0 ? prev[i] : NBW);
+          if (mo >= 0 && mo < NOUT) accb[mo % 4] = wop<T, false>(c_last, __byte_perm(d_last, D, 0x5432));
+          c_last = C;
+          d_last = D;
+        }
+        if (mo >= 0 && mo < NOUT && mo % 4 == 3) {
+          *reinterpret_cast<uint4 *>(row + OUT0 + mo - 3) = make_uint4(acca[0], acca[1], acca[2], acca[3]);
+          if constexpr (GRAD)
+            *reinterpret_cast<uint4 *>(mrow + mo - 3) = make_uint4(accb[0], accb[1], accb[2], accb[3]);
+        }
       }
     }
-    suf[W - 1] = raw[W - 1];
+    sa[W - 1] = raw[W - 1];
+    if constexpr (GRAD) sb[W - 1] = raw[W - 1];
 #pragma unroll
-    for (int i = W - 2; i >= 0; --i) suf[i] = wop<T, SUP>(suf[i + 1], raw[i]);
+    for (int i = W - 2; i >= 0; --i) {
+      sa[i] = wop<T, SA>(sa[i + 1], raw[i]);
+      if constexpr (GRAD) sb[i] = wop<T, false>(sb[i + 1], raw[i]);
+    }
 #pragma unroll
     for (int i = 0; i < W; ++i) prev[i] = raw[i];
   }
@@ -121,8 +141,8 @@ __device__ __forceinline__ void row_scan_pairs(uint32_t *row) {
 
 template <typename T, bool SUP, int K, int TW, int HW, bool GRAD>
 __device__ __forceinline__ void row_scan(uint32_t *row, uint32_t *mrow) {
-  if constexpr (sizeof(T) == 2 && !GRAD && K % 2 == 1 && HW - (K + 1) / 2 >= 0 && (HW - (K + 1) / 2) % 4 == 0) {
-    row_scan_pairs<SUP, K, TW, HW>(row);  // whole words, about half the operations per pixel
+  if constexpr (sizeof(T) == 2 && K % 2 == 1 && HW - (K + 1) / 2 >= 0 && (HW - (K + 1) / 2) % 4 == 0) {
+    row_scan_pairs<SUP, K, TW, HW, GRAD>(row, mrow);  // whole words, about half the operations per pixel
     return;
   }
   constexpr int E = 4 / (int)sizeof(T), W = 2 * K + 1;
