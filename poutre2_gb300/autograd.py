@@ -17,7 +17,7 @@ from . import _lib
 
 
 def _stream():
-    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return _lib.current_stream()
 
 
 def _planes(x: torch.Tensor):

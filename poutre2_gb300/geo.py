@@ -27,7 +27,7 @@ class reconstruction_type(enum.IntEnum):
 
 
 def _stream():
-    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return _lib.current_stream()
 
 
 def _post(check):

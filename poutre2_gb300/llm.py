@@ -18,7 +18,7 @@ from .se import Common_NL_SE, Compound_NL_SE, NeighborList
 
 
 def _stream():
-    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return _lib.current_stream()
 
 
 def _offsets(nl: NeighborList, rank: int):
