@@ -131,12 +131,9 @@ def workload_image(size):
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_hmaxima(f, budget_s=12.0, min_runs=1):
-    """Time poutre2's CPU implementation (oracle/_ref) or, failing that, the C restatement on
-    `f`; returns (pixels/s, kind, runs)."""
-    import numpy as np
-    kind = "port"
-    fn = None
+def cpu_hmaxima_fn():
+    """poutre2's CPU binary h-maxima (oracle/_ref) or, failing that, the C restatement:
+    returns (fn(image, h) -> binary image, kind)."""
     try:
         from oracle import ref
         if not ref.available():
@@ -145,13 +142,18 @@ def cpu_hmaxima(f, budget_s=12.0, min_runs=1):
             except Exception:
                 pass
         if ref.available():
-            fn = lambda: ref.h_maxima_binary(f, H_VALUE, "SESquare2D")  # noqa: E731
-            kind = "reference"
+            return (lambda img, h: ref.h_maxima_binary(img, h, "SESquare2D")), "reference"
     except Exception:
-        fn = None
-    if fn is None:
-        import oracle
-        fn = lambda: oracle.h_maxima_binary(f, H_VALUE, "SESquare2D")  # noqa: E731
+        pass
+    import oracle
+    return (lambda img, h: oracle.h_maxima_binary(img, h, "SESquare2D")), "port"
+
+
+def cpu_hmaxima(f, budget_s=12.0, min_runs=1):
+    """Time poutre2's CPU implementation (oracle/_ref) or, failing that, the C restatement on
+    `f`; returns (pixels/s, kind, runs)."""
+    hm, kind = cpu_hmaxima_fn()
+    fn = lambda: hm(f, H_VALUE)  # noqa: E731
     fn()  # warm
     times = []
     t_end = time.perf_counter() + budget_s
@@ -312,9 +314,27 @@ def extra_measurements(dev, flush, only=None):
             for x, o in zip(xs, outs):
                 geo.h_maxima_binary(x, 10, Common_NL_SE.SESquare2D, o, check=False)
         plain_ms = _time_ms(plain, flush, 3, 1)
+        kw = {}
+        try:  # poutre2 on the host: one core, and the images spread over every core (harness threads)
+            import concurrent.futures
+            hm, kind = cpu_hmaxima_fn()
+            t0 = time.perf_counter()
+            for f in imgs:
+                hm(f, 10)
+            one = (time.perf_counter() - t0) * 1e3
+            cores = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            with concurrent.futures.ThreadPoolExecutor(cores) as ex:
+                list(ex.map(lambda f: hm(f, 10), imgs))
+            par = (time.perf_counter() - t0) * 1e3
+            kw = {"cpu_kind": kind, "cpu_1core_ms": one, "cpu_parallel_ms": par, "cpu_parallel_threads": cores,
+                  "cpu_parallel_note": "harness threads over the images; poutre2 itself is single-threaded",
+                  "speedup_vs_cpu_1core": one / graph_ms, "speedup_vs_cpu_parallel": par / graph_ms}
+        except Exception as e:
+            kw = {"cpu_error": f"{type(e).__name__}: {e}"}
         rec("cfg4_ragged512_graph_replay", graph_ms, npx, 2 * npx, plain_ms=plain_ms,
             speedup_vs_plain=plain_ms / graph_ms, plan_run_ms=plan_ms, one_call_ms=one_call_ms,
-            autotuned=plan.config)
+            autotuned=plan.config, **kw)
         plan.close()
 
     def cfg5():
