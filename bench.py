@@ -17,6 +17,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -186,7 +187,9 @@ def run_reference(args):
                                    f"{args.size}x{args.size} u8 smoothed noise sigma=4 seed 1"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
                              "sample": f"{args.steps} full runs of the {args.size}^2 workload, single thread "
-                                       f"(poutre2 has no threading)"},
+                                       f"(poutre2 has no threading)",
+                             "build": f"g++ -O3 ({platform.machine()}; xsimd stand-in of fixed-width lane "
+                                      f"loops, auto-vectorised by the compiler)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -466,7 +469,9 @@ def run_gpu(args):
             v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
             line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
                                     "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
-                                              f"(poutre2 is single-threaded)"}
+                                              f"(poutre2 is single-threaded)",
+                                    "build": f"g++ -O3 ({platform.machine()}; xsimd stand-in of fixed-width lane "
+                                             f"loops, auto-vectorised by the compiler)"}
         if args.extra:
             only = set(args.only.split(",")) if args.only else None
             line["extra"] = extra_measurements(dev, flush, only)
