@@ -144,6 +144,23 @@ PG_API pg_status pg_opening(const pg_image *in, const pg_se *se, const pg_image 
 PG_API pg_status pg_closing(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
 PG_API pg_status pg_gradient(const pg_image *in, const pg_se *se, const pg_image *out, pg_stream_t stream);
 
+/* ---------------------------------------------------------------- labelling */
+
+/* poutre::label::label_binary(const IInterface&, se::Common_NL_SE, IInterface&) -> size_t,
+ * include/poutre/label/label_binary.hpp (src/label/label_binary.cpp); and label_flat_zones,
+ * include/poutre/label/label_flat_zones.hpp (src/label/label_flat_zones.cpp).  Connected components
+ * numbered 1.. by the raster position of their first pixel, 0 for the background, into `out`, an
+ * PG_PTYPE_I64 image of the input's shape.  label_binary: foreground = pixel != 0, and a pixel joins
+ * its earlier neighbours that are > 0; label_flat_zones: every pixel, joined to equal neighbours.
+ * Neighbourhood: the SE's earlier half (1D/2D SEs, SECross3D and the 3D segments; SESquare3D
+ * returns PG_ERR_UNSUPPORTED_SE).  label_binary takes u8, u16, i32, i64 images; label_flat_zones
+ * all six types.  When nb_labels is not null the call waits for the stream and writes the label
+ * count there (the reference's return value); otherwise it is asynchronous. */
+PG_API pg_status pg_label_binary(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                                 pg_stream_t stream);
+PG_API pg_status pg_label_flat_zones(const pg_image *in, int32_t common_se, const pg_image *out,
+                                     int64_t *nb_labels, pg_stream_t stream);
+
 /* ---------------------------------------------------------------- geodesy */
 
 /* poutre::geo::Reconstruction(reconstruction_type, const IInterface& marker, const IInterface& mask,
@@ -242,7 +259,8 @@ PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker,
 /* Synchronises `stream`, then returns (and clears) the device-side status of the kernels:
  * PG_ERR_NOT_CONVERGED when a reconstruction gave up (round cap or a bounded device wait), or
  * PG_ERR_CUDA when a shared-memory tile kernel (box erosion / dilation, gradient, opening) found a
- * tile load unfinished after its bounded wait, since the last check; else PG_OK.  The calls are asynchronous; call this to
+ * tile load unfinished after its bounded wait or a labelling union-find loop hit its iteration
+ * bound, since the last check; else PG_OK.  The calls are asynchronous; call this to
  * observe the failure the reference would have thrown. */
 PG_API pg_status pg_check_device(pg_stream_t stream);
 

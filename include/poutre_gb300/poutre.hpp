@@ -209,6 +209,26 @@ PG_FACADE_LEVELING(leveling)
 #undef PG_FACADE_LEVELING
 }  // namespace geo
 
+// ---------------------------------------------------------------- labelling
+namespace label {
+// poutre::label::label_binary / label_flat_zones (include/poutre/label/label_binary.hpp,
+// label_flat_zones.hpp): o_img is an INT64 image; returns the number of labels (synchronous).
+inline std::size_t label_binary(const IInterface &i_img, se::Common_NL_SE nl, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  int64_t n = 0;
+  check(pg_label_binary(&a, (int32_t)nl, &b, &n, o_img.stream()));
+  check(pg_check_device(o_img.stream()));
+  return (std::size_t)n;
+}
+inline std::size_t label_flat_zones(const IInterface &i_img, se::Common_NL_SE nl, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  int64_t n = 0;
+  check(pg_label_flat_zones(&a, (int32_t)nl, &b, &n, o_img.stream()));
+  check(pg_check_device(o_img.stream()));
+  return (std::size_t)n;
+}
+}  // namespace label
+
 // ---------------------------------------------------------------- image strings
 // "Scalar <GUINT8|GUINT16|GINT32|GINT64|F32|D64> <rank> <d0..> <values..>", as poutre's
 // ImageFromString / ImageToString (include/poutre/base/image_interface.hpp:114-122).

@@ -68,6 +68,7 @@ def lib():
             L.or_leveling_half.argtypes = [I, I, P, P, P, P, I, I]
             L.or_flat2d_forward.argtypes = [I64, I64, I64, P, P, I, I, I]
             L.or_flat2d_backward.argtypes = [I64, I64, I64, P, P, P, I, I, I]
+            L.or_label.argtypes = [I, I, P, P, P, I, I, P]
             _lib = L
     return _lib
 
@@ -303,6 +304,19 @@ def rect(img, hy, hx, dilate=True):
     DilateY(DilateX(.)) and Dilate(SESquare2D, iter=h) for hy == hx == h."""
     t = line(img, hx, "x", dilate) if hx > 0 else _c(img).copy()
     return line_y_any(t, hy, dilate) if hy > 0 else t
+
+
+# ----------------------------------------------------------------------------- labelling
+def label(img, se: str = "SESquare2D", flat_zones: bool = False):
+    """poutre::label::label_binary / label_flat_zones(i_img, Common_NL_SE, o_img)
+    (src/label/label_binary.cpp, label_flat_zones.cpp; include/poutre/label/details/label_t.hpp:132-247):
+    returns (int64 label image, number of labels)."""
+    a = _c(img)
+    out = np.empty(a.shape, dtype=np.int64)
+    count = ctypes.c_int64(0)
+    _check(lib().or_label(PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se], int(flat_zones),
+                          ctypes.byref(count)), f"label_{'flat_zones' if flat_zones else 'binary'}({se})")
+    return out, int(count.value)
 
 
 # ----------------------------------------------------------------------------- adjoint

@@ -507,6 +507,120 @@ int or_leveling_half(int pt, int rank, const int64_t *shape, const void *ref, co
 }
 
 /* ------------------------------------------------------------------------- */
+/* Connected-component labelling: poutre::label::label_binary / label_flat_zones */
+/* (include/poutre/label/details/label_t.hpp:132-247; disjoint_min_sets :87-130). */
+/* A raster scan gives each accepted pixel the provisional label of its related */
+/* upper-half neighbours (merging their sets: the smaller root wins) or a new   */
+/* one; roots are then numbered 1.. in creation order (min_label) and every     */
+/* accepted pixel takes its root's number.  mode 0: binary (accept v != 0, or   */
+/* |v| > 1e-10 for floats; a neighbour is related when it is > 0); mode 1: flat */
+/* zones (every pixel accepted; related when equal).  Returns the label count.  */
+/* A float neighbour in (0, 1e-10] is related but unlabelled: the reference    */
+/* then reads label 0 of a possibly empty set (undefined); -5 is returned.      */
+/* ------------------------------------------------------------------------- */
+static int64_t dms_find(int64_t *parents, int64_t v) {
+  int64_t p = parents[v];
+  if (parents[p] != p) parents[v] = p = dms_find(parents, p);
+  return p;
+}
+static int64_t dms_union(int64_t *parents, int64_t a, int64_t b) {
+  const int64_t ra = dms_find(parents, a), rb = dms_find(parents, b);
+  if (ra < rb) { parents[rb] = ra; return ra; }
+  if (rb < ra) { parents[ra] = rb; return rb; }
+  return ra;
+}
+
+#define DEFINE_LABEL(T, SFX, IS_FLOAT)                                                               \
+  static int label_##SFX(const int64_t d[3], const T *in, int64_t *out, const off3 *up, int nu, int mode, \
+                         int64_t *count) {                                                           \
+    const int64_t n = d[0] * d[1] * d[2];                                                            \
+    int64_t *parents = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));                 \
+    if (!parents) return -2;                                                                         \
+    int64_t np = 0;                                                                                  \
+    const int64_t sentinel = INT64_MAX;                                                              \
+    for (int64_t i = 0; i < n; ++i) out[i] = 0;                                                      \
+    int64_t i = 0;                                                                                   \
+    for (int64_t z = 0; z < d[0]; ++z)                                                               \
+      for (int64_t y = 0; y < d[1]; ++y)                                                             \
+        for (int64_t x = 0; x < d[2]; ++x, ++i) {                                                    \
+          const T v = in[i];                                                                         \
+          const int acc = mode == 1 ? 1 : (IS_FLOAT ? (fabs((double)v) > (double)ACC_EPS_##SFX) : (v != (T)0)); \
+          if (!acc) continue;                                                                        \
+          int64_t label = sentinel;                                                                  \
+          for (int k = 0; k < nu; ++k) {                                                             \
+            const int64_t j = nb_index(d, z, y, x, up[k]);                                           \
+            if (j < 0) continue;                                                                     \
+            const int rel = mode == 1 ? (v == in[j]) : (in[j] > (T)0);                               \
+            if (!rel) continue;                                                                      \
+            const int64_t nl = out[j];                                                               \
+            if (nl >= np) { free(parents); return -5; }                                              \
+            if (label == sentinel || label == nl) label = nl;                                        \
+            else label = dms_union(parents, label, nl);                                              \
+          }                                                                                          \
+          if (label == sentinel) { parents[np] = np; label = np++; }                                 \
+          out[i] = label;                                                                            \
+        }                                                                                            \
+    int64_t *num = (int64_t *)malloc(sizeof(int64_t) * (size_t)(np > 0 ? np : 1));                   \
+    if (!num) { free(parents); return -2; }                                                          \
+    int64_t c = 0;                                                                                   \
+    for (int64_t k = 0; k < np; ++k) { if (parents[k] == k) c += 1; num[k] = c; }                    \
+    for (int64_t k = 0; k < n; ++k) {                                                                \
+      const T v = in[k];                                                                             \
+      const int acc = mode == 1 ? 1 : (IS_FLOAT ? (fabs((double)v) > (double)ACC_EPS_##SFX) : (v != (T)0)); \
+      if (acc) out[k] = num[dms_find(parents, out[k])];                                              \
+    }                                                                                                \
+    *count = c;                                                                                      \
+    free(num);                                                                                       \
+    free(parents);                                                                                   \
+    return 0;                                                                                        \
+  }
+/* not_background<pFLOAT / pDOUBLE> thresholds (label_t.hpp:47-55) */
+#define ACC_EPS_u8 0
+#define ACC_EPS_u16 0
+#define ACC_EPS_i32 0
+#define ACC_EPS_i64 0
+#define ACC_EPS_f32 1E-10F
+#define ACC_EPS_f64 1E-10
+DEFINE_LABEL(uint8_t, u8, 0)
+DEFINE_LABEL(uint16_t, u16, 0)
+DEFINE_LABEL(int32_t, i32, 0)
+DEFINE_LABEL(int64_t, i64, 0)
+DEFINE_LABEL(float, f32, 1)
+DEFINE_LABEL(double, f64, 1)
+
+/* upper raster half of the SE used by the labelling (split_coordinates_upper_lower of
+ * neighbor_list_static_se_t.hpp; the segments' are their one earlier neighbour) */
+static const off3 U_SEGX[] = {{0, 0, -1}};
+static const off3 U_SEGY[] = {{0, -1, 0}};
+static const off3 U_SEGZ[] = {{-1, 0, 0}};
+static int label_upper(int se, const off3 **up, int *nu) {
+  switch (se) {
+    case SE_SEGX1D: case SE_SEGX2D: case SE_SEGX3D: *up = U_SEGX; *nu = 1; return 0;
+    case SE_SEGY2D: case SE_SEGY3D: *up = U_SEGY; *nu = 1; return 0;
+    case SE_SEGZ3D: *up = U_SEGZ; *nu = 1; return 0;
+    case SE_SQUARE2D: *up = U_SQUARE2D; *nu = 4; return 0;
+    case SE_CROSS2D: *up = U_CROSS2D; *nu = 2; return 0;
+    case SE_CROSS3D: *up = U_CROSS3D; *nu = 3; return 0;
+    case SE_SQUARE3D: *up = U_SQUARE3D; *nu = 13; return 0;
+    default: return -1;
+  }
+}
+
+int or_label(int pt, int rank, const int64_t *shape, const void *in, int64_t *out, int se, int mode,
+             int64_t *count) {
+  int64_t d[3];
+  if (dims3(rank, shape, d) < 0) return -1;
+  if (se_rank(se) != rank) return -3;
+  const off3 *up;
+  int nu;
+  if (label_upper(se, &up, &nu) < 0) return -3;
+  int rc = 0;
+#define CALL_LB(T, S) rc = label_##S(d, (const T *)in, out, up, nu, mode, count)
+  DISPATCH(pt, CALL_LB)
+  return rc;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Flat 2D morphology on float32 planes with the first-in-scan-order arg      */
 /* routing used for the adjoint (no counterpart in the reference; the forward */
 /* is Dilate/Erode by a (2r+1)^2 square, which for r=2 equals                 */

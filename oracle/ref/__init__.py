@@ -41,6 +41,8 @@ def lib():
         L.ref_extrema.argtypes = [I, I, I, P, P, P, D, I]
         L.ref_h_maxima_binary.argtypes = [I, P, P, P, D, I]
         L.ref_leveling.argtypes = [I, I, I, P, P, P, P, I]
+        if hasattr(L, "ref_label"):
+            L.ref_label.argtypes = [I, I, I, P, P, P, I, P]
         _lib = L
     return _lib
 
@@ -103,3 +105,13 @@ def leveling(kind, ref, marker, se="SESquare2D"):
     k = {"low_leveling": 0, "high_leveling": 1, "leveling": 2}[kind]
     _chk(lib().ref_leveling(k, PTYPE[r.dtype], r.ndim, _shape(r), _p(r), _p(m), _p(out), SE[se]))
     return out
+
+
+def label(img, se="SESquare2D", flat_zones=False):
+    """poutre::label::label_binary / label_flat_zones on the compiled reference:
+    returns (int64 label image, number of labels)."""
+    a = np.ascontiguousarray(img)
+    out = np.empty(a.shape, dtype=np.int64)
+    n = ctypes.c_int64(0)
+    _chk(lib().ref_label(int(flat_zones), PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se], ctypes.byref(n)))
+    return out, int(n.value)

@@ -4,8 +4,8 @@ TEST INFRASTRUCTURE ONLY (checker + CPU baseline).  Recipe:
 
 1. ``stage``: when the poutre2 tree is available (``POUTRE2_REFERENCE``, default
    ``/root/reference``), copy the headers under ``include/poutre`` and the ``.cpp`` files
-   of the five modules on the path (base, pixel_processing, structuring_element,
-   low_level_morpho, geodesy) into ``oracle/_ref/src``.  ``oracle/_ref`` is git-ignored,
+   of the modules on the path (base, pixel_processing, structuring_element,
+   low_level_morpho, geodesy) and of label into ``oracle/_ref/src``.  ``oracle/_ref`` is git-ignored,
    so no reference source enters the repository; the staged copy only lets the same
    recipe run on a machine that does not mount the tree (the aarch64 GPU host).
 2. ``compile``: ``g++ -std=c++23 -O3`` on the staged sources plus ``ref_harness.cpp``,
@@ -31,7 +31,7 @@ OUT = os.path.join(ORACLE, "_ref")
 STAGE = os.path.join(OUT, "src")
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libpoutre_ref.so")
-MODULES = ["base", "pixel_processing", "structuring_element", "low_level_morpho", "geodesy"]
+MODULES = ["base", "pixel_processing", "structuring_element", "low_level_morpho", "geodesy", "label"]
 
 
 def reference_root():

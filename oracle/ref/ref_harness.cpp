@@ -11,6 +11,8 @@
 #include <poutre/geodesy/extrema.hpp>
 #include <poutre/geodesy/leveling.hpp>
 #include <poutre/geodesy/mreconstruct.hpp>
+#include <poutre/label/label_binary.hpp>
+#include <poutre/label/label_flat_zones.hpp>
 #include <poutre/low_level_morpho/ero_dil.hpp>
 #include <poutre/low_level_morpho/ero_dil_line.hpp>
 #include <poutre/pixel_processing/compare.hpp>
@@ -190,6 +192,19 @@ int ref_reconstruct(int pt, int rank, const int64_t *shape, const void *marker, 
                                        : poutre::geo::reconstruction_type::erode,
                                 *m, *k, static_cast<poutre::se::Common_NL_SE>(se), *o);
     take(*o, pt, rank, shape, out);
+  });
+}
+
+// poutre::label::label_binary (flat = 0) / label_flat_zones (flat = 1),
+// include/poutre/label/label_binary.hpp, label_flat_zones.hpp: int64 labels into out, count into *n.
+int ref_label(int flat, int pt, int rank, const int64_t *shape, const void *in, int64_t *out, int se, int64_t *n) {
+  return guarded([&] {
+    auto a = make(pt, rank, shape, in);
+    auto o = make(32, rank, shape, nullptr);
+    auto s = static_cast<poutre::se::Common_NL_SE>(se);
+    const std::size_t c = flat ? poutre::label::label_flat_zones(*a, s, *o) : poutre::label::label_binary(*a, s, *o);
+    take(*o, 32, rank, shape, out);
+    *n = static_cast<int64_t>(c);
   });
 }
 

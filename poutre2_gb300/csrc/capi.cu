@@ -316,6 +316,25 @@ static pg_status h_recon(const pg_image *in, double h, int se, const pg_image *o
   return launch_reconstruction(nullptr, in, out, 1, rq, s);
 }
 
+// ---------------------------------------------------------------- labelling
+// poutre::label::label_binary / label_flat_zones (src/label/label_binary.cpp, label_flat_zones.cpp):
+// the output is an INT64 image of the input's shape (the reference's dispatch downcasts it to
+// image_t<int64>), distinct from the input; the SE's rank must be the image's.
+static pg_status label_call(const pg_image *in, int32_t se, const pg_image *out, int64_t *nb_labels, bool flat,
+                            cudaStream_t s) {
+  const char *what = flat ? "label_flat_zones" : "label_binary";
+  PG_TRY(check_image(in, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " incompatible size");
+  if (out->ptype != PG_PTYPE_I64)
+    return fail(PG_ERR_INCOMPATIBLE, std::string(what) + "ImageDispatch o_img downcast fail (output must be INT64)");
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, std::string(what) + " input output images must be different");
+  if (se_rank(se) == 0 || se_rank(se) != in->rank)
+    return fail(PG_ERR_UNSUPPORTED_SE, flat ? "t_label_flat_zonesDispatch unsupported nl_static"
+                                            : "t_label_binaryDispatch unsupported nl_static");
+  return launch_label(*in, se, *out, flat, nb_labels, s);
+}
+
 }  // namespace pg
 
 using namespace pg;
@@ -400,6 +419,15 @@ pg_status pg_gradient(const pg_image *in, const pg_se *se, const pg_image *out, 
   PG_TRY(check_in_out(in, out, "Gradient"));
   if (!se) return fail(PG_ERR_INVALID_ARGUMENT, "null SE");
   return composite(*in, *se, *out, C_GRAD, STREAM(s));
+}
+
+pg_status pg_label_binary(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                          pg_stream_t s) {
+  return label_call(in, common_se, out, nb_labels, false, STREAM(s));
+}
+pg_status pg_label_flat_zones(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                              pg_stream_t s) {
+  return label_call(in, common_se, out, nb_labels, true, STREAM(s));
 }
 
 // ---------------------------------------------------------------- geodesy

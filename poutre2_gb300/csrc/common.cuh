@@ -202,6 +202,9 @@ bool try_rect_gradient(const pg_image &in, const pg_image &out, int64_t hy, int6
 bool try_rect_open(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool opening, cudaStream_t s,
                    pg_status *st);
 int take_open_status();  // device status of the one-pass opening kernel since the last call (0: none)
+// connected-component labelling into an int64 image (label.cu); count may be null
+pg_status launch_label(const pg_image &in, int se, const pg_image &out, bool flat, int64_t *count, cudaStream_t s);
+int take_label_status();
 int take_rect_status();  // device status of the fused square kernel since the last call (0: none)
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);

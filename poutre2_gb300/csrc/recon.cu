@@ -1608,6 +1608,8 @@ pg_status pg_check_device(pg_stream_t stream) {
     return pg::fail(static_cast<pg_status>(rs), "a box tile load did not complete within its wait limit");
   if (const int os = pg::take_open_status())
     return pg::fail(static_cast<pg_status>(os), "an opening tile load did not complete within its wait limit");
+  if (const int ls = pg::take_label_status())
+    return pg::fail(static_cast<pg_status>(ls), "a labelling union-find loop exceeded its iteration limit");
   return PG_OK;
 }
 

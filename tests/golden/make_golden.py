@@ -2,7 +2,7 @@
 
 Reads poutre2's Catch2 test sources *as text* (no reference code is built or run):
 every test case there parses its inputs with ``poutre::ImageFromString``, calls one
-hot-path entry point and compares ``ImageToString(out)`` with an expected string.
+hot-path (or labelling) entry point and compares ``ImageToString(out)`` with an expected string.
 This script records, per case, the source file:line, the entry point, its
 structuring element / scalar parameter, the input images and the expected image.
 
@@ -23,6 +23,8 @@ FILES = [
     "test/geodesy/mreconstruct.cpp",
     "test/geodesy/extrema.cpp",
     "test/geodesy/leveling.cpp",
+    "test/label/label_binary.cpp",
+    "test/label/label_flat_zones.cpp",
 ]
 
 # image-string tokens -> numpy dtype names (src/base/types.cpp:295-341)
@@ -30,7 +32,7 @@ PTYPES = {"GUINT8": "uint8", "GINT32": "int32", "GINT64": "int64", "F32": "float
 
 OPS = (
     r"t_DilateX|t_ErodeX|t_DilateY|t_ErodeY|t_Dilate|t_Erode|Reconstruction|h_minima|h_maxima|h_convex|h_concave|"
-    r"dynamic_pseudo_opening|dynamic_pseudo_closing|low_leveling|high_leveling|leveling"
+    r"dynamic_pseudo_opening|dynamic_pseudo_closing|low_leveling|high_leveling|leveling|label_binary|label_flat_zones"
 )
 
 TOKEN = re.compile(
@@ -123,7 +125,8 @@ def main():
     cases = extract(root)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(out, "w") as f:
-        json.dump({"source": "poutre2 Catch2 tests (test/low_level_morpho, test/geodesy)", "cases": cases}, f, indent=1)
+        json.dump({"source": "poutre2 Catch2 tests (test/low_level_morpho, test/geodesy, test/label)", "cases": cases},
+                  f, indent=1)
     print(f"wrote {len(cases)} cases to {out}")
 
 

@@ -84,3 +84,30 @@ def test_synthetic_inputs_are_deterministic():
     assert np.array_equal(a, b) and a.min() == 0 and a.max() == 255
     sizes = synthetic.ragged_sizes(512)
     assert len(sizes) == 512 and all(64 <= h <= 1024 and 64 <= w <= 1024 for h, w in sizes)
+
+
+def test_labelling_argument_checks_need_no_gpu(lib_path):
+    # the C ABI rejects, before any device work, what the reference rejects: an output that is not
+    # INT64, an SE of another rank, SESquare3D (not on the GPU path), a float image for label_binary
+    import ctypes
+    from poutre2_gb300 import _lib
+    L = _lib.load()
+
+    def img(ptype, shape):
+        d = _lib.PgImage()
+        d.data, d.ptype, d.rank = 0x1000, ptype, len(shape)
+        for i, s in enumerate(shape):
+            d.shape[i] = s
+        return d
+
+    n = ctypes.c_int64(0)
+    a, o = img(4, (8, 8)), img(32, (8, 8))
+    o.data = 0x100000
+    assert L.pg_label_binary(ctypes.byref(a), 2, ctypes.byref(img(4, (8, 8))), ctypes.byref(n), None) == 4  # u8 out
+    assert L.pg_label_binary(ctypes.byref(a), 9, ctypes.byref(o), ctypes.byref(n), None) == 3  # 3D SE, 2D image
+    a3, o3 = img(4, (4, 4, 4)), img(32, (4, 4, 4))
+    o3.data = 0x100000
+    assert L.pg_label_binary(ctypes.byref(a3), 10, ctypes.byref(o3), ctypes.byref(n), None) == 3  # SESquare3D
+    af = img(16, (8, 8))
+    assert L.pg_label_binary(ctypes.byref(af), 2, ctypes.byref(o), ctypes.byref(n), None) == 2  # float binary
+    assert L.pg_label_flat_zones(ctypes.byref(a), 2, ctypes.byref(img(32, (8, 9))), ctypes.byref(n), None) == 4

@@ -64,6 +64,11 @@ def test_reference_kat_on_gpu(case):
                            ins[0], ins[1], Common_NL_SE[case["se"]], out)
     elif op in ("low_leveling", "high_leveling", "leveling"):
         getattr(geo, op)(ins[0], ins[1], Common_NL_SE[case["se"]], out)
+    elif op in ("label_binary", "label_flat_zones"):
+        from poutre2_gb300 import label
+        out = torch.empty(ins[0].shape, dtype=torch.int64, device=ins[0].device)
+        n = getattr(label, op)(ins[0], Common_NL_SE[case["se"]], out)
+        assert n == int(exp.max())
     else:
         getattr(geo, op)(ins[0], case["h"], Common_NL_SE[case["se"]], out)
     np.testing.assert_array_equal(host(out), exp)
@@ -564,3 +569,64 @@ def test_empty_images_are_accepted(shape):
     geo.h_maxima_binary_batch([x, y], 3, Common_NL_SE.SESquare2D, [out, oy])
     np.testing.assert_array_equal(host(oy), oracle.h_maxima_binary(np.zeros((3, 4), np.uint8), 3, "SESquare2D"))
     torch.cuda.synchronize()
+
+
+# ----------------------------------------------------------------------------- labelling
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.int64, np.float32, np.float64])
+@pytest.mark.parametrize("se,rank", [("SESquare2D", 2), ("SECross2D", 2), ("SESegmentX2D", 2), ("SESegmentY2D", 2),
+                                     ("SESegmentX1D", 1), ("SECross3D", 3), ("SESegmentX3D", 3), ("SESegmentZ3D", 3)])
+@pytest.mark.parametrize("flat", [False, True])
+def test_labelling(dt, se, rank, flat):
+    from poutre2_gb300 import label
+    from poutre2_gb300.se import Common_NL_SE
+    if not flat and np.dtype(dt).kind == "f":
+        pytest.skip("label_binary of float images is not on the GPU path")
+    rng = np.random.default_rng(abs(hash((str(dt), se, flat))) % 2**32)
+    shapes = {1: [(1,), (50,), (5000,)], 2: [(1, 1), (17, 33), (130, 257)], 3: [(1, 1, 1), (6, 7, 9), (20, 33, 40)]}[rank]
+    for shape in shapes:
+        if flat:
+            a = rng.integers(0, 3, shape).astype(dt)
+        else:
+            fg = rng.random(shape) < 0.5
+            vals = rng.integers(-2 if np.dtype(dt).kind == "i" else 1, 5, shape)
+            a = (fg * vals).astype(dt)
+        out = torch.empty(shape, dtype=torch.int64, device="cuda")
+        n = (label.label_flat_zones if flat else label.label_binary)(dev(a), Common_NL_SE[se], out)
+        exp, m = oracle.label(a, se, flat)
+        assert n == m, shape
+        np.testing.assert_array_equal(host(out), exp, err_msg=f"{shape}")
+
+
+def test_labelling_of_h_maxima_2048():
+    # the binary h-maxima of the headline image, labelled: many components of every size
+    from poutre2_gb300 import geo, label, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    f = synthetic.smoothed_noise_u8((2048, 2048), 1, 4.0)
+    x = dev(f)
+    b = torch.empty_like(x)
+    geo.h_maxima_binary(x, 20, Common_NL_SE.SESquare2D, b)
+    for se in ("SESquare2D", "SECross2D"):
+        out = torch.empty(x.shape, dtype=torch.int64, device="cuda")
+        n = label.label_binary(b, Common_NL_SE[se], out)
+        exp, m = oracle.label(host(b), se, False)
+        assert n == m and n > 100
+        np.testing.assert_array_equal(host(out), exp)
+    out = torch.empty(x.shape, dtype=torch.int64, device="cuda")
+    n = label.label_flat_zones(x, Common_NL_SE.SESquare2D, out)
+    exp, m = oracle.label(f, "SESquare2D", True)
+    assert n == m
+    np.testing.assert_array_equal(host(out), exp)
+
+
+def test_labelling_rejects_like_the_reference():
+    from poutre2_gb300 import label
+    from poutre2_gb300._lib import PoutreError
+    from poutre2_gb300.se import Common_NL_SE
+    x = dev(np.ones((8, 8), np.uint8))
+    with pytest.raises(PoutreError):
+        label.label_binary(x, Common_NL_SE.SESquare2D, torch.empty_like(x))  # output must be int64
+    with pytest.raises(PoutreError):
+        label.label_binary(x, Common_NL_SE.SECross3D, torch.empty(8, 8, dtype=torch.int64, device="cuda"))
+    v = dev(np.ones((4, 4, 4), np.uint8))
+    with pytest.raises(PoutreError):
+        label.label_binary(v, Common_NL_SE.SESquare3D, torch.empty(4, 4, 4, dtype=torch.int64, device="cuda"))

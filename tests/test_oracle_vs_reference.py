@@ -145,3 +145,29 @@ def test_uint16_composition_rule():
         np.testing.assert_array_equal(got, exp)
     b = a[:29, :29].copy()  # DilateY/ErodeY need a square image
     np.testing.assert_array_equal(oracle.line(b, 5, "y", False), ref.line(b.astype(np.int32), 5, "y", False).astype(np.uint16))
+
+
+@pytest.mark.parametrize("dt", REF_TYPES)
+@pytest.mark.parametrize("se,rank", [("SESquare2D", 2), ("SECross2D", 2), ("SESegmentX2D", 2), ("SESegmentY2D", 2),
+                                     ("SESegmentX1D", 1), ("SECross3D", 3), ("SESegmentZ3D", 3)])
+@pytest.mark.parametrize("flat", [False, True])
+def test_labelling(dt, se, rank, flat):
+    # label_binary with negative and zero pixels (a negative pixel is foreground but joins no later
+    # pixel), and label_flat_zones over a few grey levels
+    rng = np.random.default_rng(hash((str(dt), se, flat)) % 2**32)
+    for shape in ([(1,), (37,), (200,)] if rank == 1 else [(1, 1), (9, 13), (64, 41)] if rank == 2
+                  else [(1, 1, 1), (5, 6, 7), (9, 12, 11)])[: 3]:
+        shape = shape[:rank]
+        if flat:
+            a = rng.integers(0, 3, shape).astype(dt)
+        else:
+            fg = rng.random(shape) < 0.45
+            vals = rng.integers(-2 if np.dtype(dt).kind in "if" else 1, 5, shape)
+            a = (fg * vals).astype(dt)
+        try:
+            got, n = oracle.label(a, se, flat)
+        except oracle.OracleError:
+            continue  # float background in (0, 1e-10]: undefined in the reference
+        exp, m = ref.label(a, se, flat)
+        assert n == m
+        np.testing.assert_array_equal(got, exp)
