@@ -217,7 +217,8 @@ def _time_ms(fn, flush, reps=5, warm=2):
 
 def extra_measurements(dev, flush, only=None):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
-    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5), or all."""
+    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048), or
+    all."""
     import numpy as np
     import torch
 
@@ -359,7 +360,32 @@ def extra_measurements(dev, flush, only=None):
             rec(f"cfg5_{name}_5x5_fwd_bwd_64x32x256x256_f32", fb_ms, n, passes * 5 * n * 4, fwd_bwd_over_fwd=fb_ms / fwd)
             del xr
 
-    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5):
+    def label2048():
+        # labelling (the next row after the configs): the binary h-maxima of the headline image, and
+        # the flat zones of the image itself, against poutre2 on one host core
+        from poutre2_gb300 import label
+        f = synthetic.smoothed_noise_u8((2048, 2048), 1, 4.0)
+        x = torch.from_numpy(f).to(dev)
+        b = torch.empty_like(x)
+        geo.h_maxima_binary(x, H_VALUE, Common_NL_SE.SESquare2D, b)
+        out = torch.empty(x.shape, dtype=torch.int64, device=dev)
+        bh = b.cpu().numpy()
+        for name, img, host_img, flat in (("label_binary_hmaxima", b, bh, False), ("label_flat_zones", x, f, True)):
+            fn = label.label_flat_zones if flat else label.label_binary
+            ms = _time_ms(lambda fn=fn, img=img: fn(img, Common_NL_SE.SESquare2D, out), flush, 5, 2)
+            kw = {"note": "includes the synchronous read-back of the label count"}
+            try:
+                from oracle import ref
+                if ref.available():
+                    t0 = time.perf_counter()
+                    ref.label(host_img, "SESquare2D", flat)
+                    kw.update(cpu_ms=(time.perf_counter() - t0) * 1e3, cpu_kind="reference")
+                    kw["speedup_vs_cpu"] = kw["cpu_ms"] / ms
+            except Exception:
+                pass
+            rec(f"{name}_2048_u8", ms, img.numel(), img.numel() * 9, **kw)
+
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048):
         if only is None or fn.__name__ in only:
             guard(fn)
     return res
