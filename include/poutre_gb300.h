@@ -161,6 +161,15 @@ PG_API pg_status pg_label_binary(const pg_image *in, int32_t common_se, const pg
 PG_API pg_status pg_label_flat_zones(const pg_image *in, int32_t common_se, const pg_image *out,
                                      int64_t *nb_labels, pg_stream_t stream);
 
+/* poutre::label::label_minima / label_maxima(const IInterface&, se::Common_NL_SE, IInterface&),
+ * include/poutre/label/label_extrema.hpp (src/label/label_extrema.cpp): the regional minima /
+ * maxima, labelled: label_binary of h_concave(f, 1) / h_convex(f, 1).  Integer images; SEs of the
+ * reconstruction (SESegmentX1D, SESquare2D, SECross2D); output and nb_labels as label_binary. */
+PG_API pg_status pg_label_minima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                                 pg_stream_t stream);
+PG_API pg_status pg_label_maxima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                                 pg_stream_t stream);
+
 /* ---------------------------------------------------------------- geodesy */
 
 /* poutre::geo::Reconstruction(reconstruction_type, const IInterface& marker, const IInterface& mask,

@@ -227,6 +227,17 @@ inline std::size_t label_flat_zones(const IInterface &i_img, se::Common_NL_SE nl
   check(pg_check_device(o_img.stream()));
   return (std::size_t)n;
 }
+// poutre::label::label_minima / label_maxima (include/poutre/label/label_extrema.hpp)
+inline void label_minima(const IInterface &i_img, se::Common_NL_SE nl, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_label_minima(&a, (int32_t)nl, &b, nullptr, o_img.stream()));
+  check(pg_check_device(o_img.stream()));
+}
+inline void label_maxima(const IInterface &i_img, se::Common_NL_SE nl, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_label_maxima(&a, (int32_t)nl, &b, nullptr, o_img.stream()));
+  check(pg_check_device(o_img.stream()));
+}
 }  // namespace label
 
 // ---------------------------------------------------------------- image strings

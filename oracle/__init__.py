@@ -319,6 +319,13 @@ def label(img, se: str = "SESquare2D", flat_zones: bool = False):
     return out, int(count.value)
 
 
+def label_extrema(img, se: str = "SESquare2D", maxima: bool = False):
+    """poutre::label::label_minima / label_maxima (src/label/label_extrema.cpp): label_binary of
+    h_concave(f, 1) / h_convex(f, 1); returns (int64 label image, number of labels)."""
+    ext = h_convex(img, 1, se) if maxima else h_concave(img, 1, se)
+    return label(ext, se)
+
+
 # ----------------------------------------------------------------------------- adjoint
 def flat2d_forward(x, r: int, dilate: bool):
     a = np.ascontiguousarray(x, dtype=np.float32)

@@ -43,6 +43,8 @@ def lib():
         L.ref_leveling.argtypes = [I, I, I, P, P, P, P, I]
         if hasattr(L, "ref_label"):
             L.ref_label.argtypes = [I, I, I, P, P, P, I, P]
+        if hasattr(L, "ref_label_extrema"):
+            L.ref_label_extrema.argtypes = [I, I, I, P, P, P, I]
         _lib = L
     return _lib
 
@@ -115,3 +117,11 @@ def label(img, se="SESquare2D", flat_zones=False):
     n = ctypes.c_int64(0)
     _chk(lib().ref_label(int(flat_zones), PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se], ctypes.byref(n)))
     return out, int(n.value)
+
+
+def label_extrema(img, se="SESquare2D", maxima=False):
+    """poutre::label::label_minima / label_maxima on the compiled reference: the int64 label image."""
+    a = np.ascontiguousarray(img)
+    out = np.empty(a.shape, dtype=np.int64)
+    _chk(lib().ref_label_extrema(int(maxima), PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se]))
+    return out

@@ -12,6 +12,7 @@
 #include <poutre/geodesy/leveling.hpp>
 #include <poutre/geodesy/mreconstruct.hpp>
 #include <poutre/label/label_binary.hpp>
+#include <poutre/label/label_extrema.hpp>
 #include <poutre/label/label_flat_zones.hpp>
 #include <poutre/low_level_morpho/ero_dil.hpp>
 #include <poutre/low_level_morpho/ero_dil_line.hpp>
@@ -205,6 +206,19 @@ int ref_label(int flat, int pt, int rank, const int64_t *shape, const void *in, 
     const std::size_t c = flat ? poutre::label::label_flat_zones(*a, s, *o) : poutre::label::label_binary(*a, s, *o);
     take(*o, 32, rank, shape, out);
     *n = static_cast<int64_t>(c);
+  });
+}
+
+// poutre::label::label_minima (maxima = 0) / label_maxima (maxima = 1),
+// include/poutre/label/label_extrema.hpp: int64 labels into out (the reference returns no count).
+int ref_label_extrema(int maxima, int pt, int rank, const int64_t *shape, const void *in, int64_t *out, int se) {
+  return guarded([&] {
+    auto a = make(pt, rank, shape, in);
+    auto o = make(32, rank, shape, nullptr);
+    auto s = static_cast<poutre::se::Common_NL_SE>(se);
+    if (maxima) poutre::label::label_maxima(*a, s, *o);
+    else poutre::label::label_minima(*a, s, *o);
+    take(*o, 32, rank, shape, out);
   });
 }
 

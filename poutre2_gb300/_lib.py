@@ -25,7 +25,7 @@ EXPORTED = [
     "pg_erode", "pg_dilate", "pg_erode_compound", "pg_dilate_compound", "pg_erode_nl", "pg_dilate_nl",
     "pg_erode_x", "pg_dilate_x", "pg_erode_y", "pg_dilate_y",
     "pg_erode_se", "pg_dilate_se", "pg_opening", "pg_closing", "pg_gradient",
-    "pg_label_binary", "pg_label_flat_zones",
+    "pg_label_binary", "pg_label_flat_zones", "pg_label_minima", "pg_label_maxima",
     "pg_reconstruction", "pg_h_minima", "pg_h_maxima", "pg_h_concave", "pg_h_convex",
     "pg_dynamic_pseudo_opening", "pg_dynamic_pseudo_closing", "pg_h_maxima_binary", "pg_h_maxima_binary_batch",
     "pg_low_leveling", "pg_high_leveling", "pg_leveling",
@@ -85,6 +85,8 @@ def load(path: str | None = None):
             "pg_opening": [img, se, img, VP], "pg_closing": [img, se, img, VP], "pg_gradient": [img, se, img, VP],
             "pg_label_binary": [img, I32, img, ctypes.POINTER(I64), VP],
             "pg_label_flat_zones": [img, I32, img, ctypes.POINTER(I64), VP],
+            "pg_label_minima": [img, I32, img, ctypes.POINTER(I64), VP],
+            "pg_label_maxima": [img, I32, img, ctypes.POINTER(I64), VP],
             "pg_reconstruction": [I32, img, img, I32, img, VP],
             "pg_h_minima": [img, D, I32, img, VP], "pg_h_maxima": [img, D, I32, img, VP],
             "pg_h_concave": [img, D, I32, img, VP], "pg_h_convex": [img, D, I32, img, VP],

@@ -316,6 +316,35 @@ static pg_status h_recon(const pg_image *in, double h, int se, const pg_image *o
   return launch_reconstruction(nullptr, in, out, 1, rq, s);
 }
 
+// poutre::label::label_minima / label_maxima (src/label/label_extrema.cpp): label_binary of
+// h_concave(f, 1) / h_convex(f, 1) -- the regional minima / maxima, numbered in raster order.
+static pg_status label_extrema(const pg_image *in, int32_t se, const pg_image *out, int64_t *nb_labels, bool maxima,
+                               cudaStream_t s) {
+  const char *what = maxima ? "label_maxima" : "label_minima";
+  PG_TRY(check_image(in, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " incompatible size");
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, std::string(what) + " output must be != than input images");
+  if (out->ptype != PG_PTYPE_I64)
+    return fail(PG_ERR_INCOMPATIBLE, "label_binaryImageDispatch o_img downcast fail (output must be INT64)");
+  if (in->ptype == PG_PTYPE_F32 || in->ptype == PG_PTYPE_F64)
+    return fail(PG_ERR_UNSUPPORTED_PTYPE, "label_binary of a float image is not on the GPU path");
+  if (se_rank(se) == 0 || se_rank(se) != in->rank) return fail(PG_ERR_UNSUPPORTED_SE, "t_label_binaryDispatch unsupported nl_static");
+  bool conn8;
+  PG_TRY(recon_se(se, in->rank, conn8));  // the h-extrema reconstruction's own SE rule
+  const size_t bytes = (size_t)dims_of(*in).count() * elem_size(in->ptype);
+  Scratch rec, ext;
+  PG_TRY(rec.alloc(bytes, s));
+  PG_TRY(ext.alloc(bytes, s));
+  pg_image r = *in, e = *in;
+  r.data = rec.ptr;
+  e.data = ext.ptr;
+  PG_TRY(h_recon(in, 1.0, se, &r, maxima, s));  // h_maxima / h_minima with h = 1
+  // h_convex = sat_sub(f, h_maxima(f)), h_concave = sat_sub(h_minima(f), f) (extrema.cpp:51-73)
+  PG_TRY(maxima ? launch_sat_sub_image(*in, r, e, s) : launch_sat_sub_image(r, *in, e, s));
+  return launch_label(e, se, *out, false, nb_labels, s);
+}
+
 // ---------------------------------------------------------------- labelling
 // poutre::label::label_binary / label_flat_zones (src/label/label_binary.cpp, label_flat_zones.cpp):
 // the output is an INT64 image of the input's shape (the reference's dispatch downcasts it to
@@ -428,6 +457,14 @@ pg_status pg_label_binary(const pg_image *in, int32_t common_se, const pg_image 
 pg_status pg_label_flat_zones(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
                               pg_stream_t s) {
   return label_call(in, common_se, out, nb_labels, true, STREAM(s));
+}
+pg_status pg_label_minima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                          pg_stream_t s) {
+  return label_extrema(in, common_se, out, nb_labels, false, STREAM(s));
+}
+pg_status pg_label_maxima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
+                          pg_stream_t s) {
+  return label_extrema(in, common_se, out, nb_labels, true, STREAM(s));
 }
 
 // ---------------------------------------------------------------- geodesy

@@ -34,3 +34,14 @@ def label_flat_zones(i_img: torch.Tensor, nl_static, o_img: torch.Tensor) -> int
     """poutre::label::label_flat_zones(i_img, Common_NL_SE, o_img) -> number of labels
     (src/label/label_flat_zones.cpp): every pixel, joined to equal neighbours."""
     return _label("pg_label_flat_zones", i_img, nl_static, o_img)
+
+
+def label_minima(i_img: torch.Tensor, nl_static, o_img: torch.Tensor) -> int:
+    """poutre::label::label_minima(i_img, Common_NL_SE, o_img) (src/label/label_extrema.cpp):
+    label_binary of h_concave(i_img, 1); returns the number of labels (the reference returns none)."""
+    return _label("pg_label_minima", i_img, nl_static, o_img)
+
+
+def label_maxima(i_img: torch.Tensor, nl_static, o_img: torch.Tensor) -> int:
+    """poutre::label::label_maxima(i_img, Common_NL_SE, o_img): label_binary of h_convex(i_img, 1)."""
+    return _label("pg_label_maxima", i_img, nl_static, o_img)

@@ -102,6 +102,8 @@ int main(int argc, char **argv) {
       else if (op == "dynamic_pseudo_closing") geo::dynamic_pseudo_closing(a, param, se_of(sen), o);
       else if (op == "label_binary") label::label_binary(a, se_of(sen), o);  // int64 in, int64 out
       else if (op == "label_flat_zones") label::label_flat_zones(a, se_of(sen), o);
+      else if (op == "label_minima") label::label_minima(a, se_of(sen), o);
+      else if (op == "label_maxima") label::label_maxima(a, se_of(sen), o);
       else { std::cerr << "unknown op " << op << "\n"; return 102; }
       ++run;
       const std::string got = ImageToString(o);

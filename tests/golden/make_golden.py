@@ -25,6 +25,7 @@ FILES = [
     "test/geodesy/leveling.cpp",
     "test/label/label_binary.cpp",
     "test/label/label_flat_zones.cpp",
+    "test/label/label_extrema.cpp",
 ]
 
 # image-string tokens -> numpy dtype names (src/base/types.cpp:295-341)
@@ -32,7 +33,8 @@ PTYPES = {"GUINT8": "uint8", "GINT32": "int32", "GINT64": "int64", "F32": "float
 
 OPS = (
     r"t_DilateX|t_ErodeX|t_DilateY|t_ErodeY|t_Dilate|t_Erode|Reconstruction|h_minima|h_maxima|h_convex|h_concave|"
-    r"dynamic_pseudo_opening|dynamic_pseudo_closing|low_leveling|high_leveling|leveling|label_binary|label_flat_zones"
+    r"dynamic_pseudo_opening|dynamic_pseudo_closing|low_leveling|high_leveling|leveling|label_binary|label_flat_zones|"
+    r"label_minima|label_maxima"
 )
 
 TOKEN = re.compile(

@@ -111,3 +111,10 @@ def test_labelling_argument_checks_need_no_gpu(lib_path):
     af = img(16, (8, 8))
     assert L.pg_label_binary(ctypes.byref(af), 2, ctypes.byref(o), ctypes.byref(n), None) == 2  # float binary
     assert L.pg_label_flat_zones(ctypes.byref(a), 2, ctypes.byref(img(32, (8, 9))), ctypes.byref(n), None) == 4
+    o8 = img(4, (8, 8))
+    o8.data = 0x100000
+    for fn in (L.pg_label_minima, L.pg_label_maxima):
+        assert fn(ctypes.byref(a), 2, ctypes.byref(o8), ctypes.byref(n), None) == 4  # u8 out
+        assert fn(ctypes.byref(a), 2, ctypes.byref(a), ctypes.byref(n), None) == 5  # in place
+        assert fn(ctypes.byref(a), 9, ctypes.byref(o), ctypes.byref(n), None) == 3  # 3D SE, 2D image
+        assert fn(ctypes.byref(af), 2, ctypes.byref(o), ctypes.byref(n), None) == 2  # float image

@@ -49,4 +49,4 @@ def test_facade_replays_reference_kats(tmp_path):
     cases.write_text("\n".join(lines) + "\n")
     r = subprocess.run([exe, str(cases)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "66 cases, 0 failed" in r.stdout
+    assert "68 cases, 0 failed" in r.stdout

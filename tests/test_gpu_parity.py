@@ -64,7 +64,7 @@ def test_reference_kat_on_gpu(case):
                            ins[0], ins[1], Common_NL_SE[case["se"]], out)
     elif op in ("low_leveling", "high_leveling", "leveling"):
         getattr(geo, op)(ins[0], ins[1], Common_NL_SE[case["se"]], out)
-    elif op in ("label_binary", "label_flat_zones"):
+    elif op in ("label_binary", "label_flat_zones", "label_minima", "label_maxima"):
         from poutre2_gb300 import label
         out = torch.empty(ins[0].shape, dtype=torch.int64, device=ins[0].device)
         n = getattr(label, op)(ins[0], Common_NL_SE[case["se"]], out)
@@ -616,6 +616,38 @@ def test_labelling_of_h_maxima_2048():
     exp, m = oracle.label(f, "SESquare2D", True)
     assert n == m
     np.testing.assert_array_equal(host(out), exp)
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16, np.int32, np.int64])
+@pytest.mark.parametrize("se", ["SESquare2D", "SECross2D", "SESegmentX1D"])
+@pytest.mark.parametrize("maxima", [False, True])
+def test_label_extrema(dt, se, maxima):
+    # label_minima / label_maxima (label_binary of h_concave / h_convex with h = 1) on plateau-rich
+    # images, where regional extrema are flat zones of many shapes
+    from poutre2_gb300 import label
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(hash((str(dt), se, maxima)) % 2**32)
+    shapes = [(1,), (77,), (4099,)] if se.endswith("1D") else [(1, 1), (19, 23), (200, 333)]
+    for shape in shapes:
+        a = rng.integers(0, 6, shape).astype(dt)
+        out = torch.empty(shape, dtype=torch.int64, device="cuda")
+        n = (label.label_maxima if maxima else label.label_minima)(dev(a), Common_NL_SE[se], out)
+        exp, m = oracle.label_extrema(a, se, maxima)
+        assert n == m, shape
+        np.testing.assert_array_equal(host(out), exp, err_msg=f"{shape}")
+
+
+def test_label_extrema_2048():
+    from poutre2_gb300 import label, synthetic
+    from poutre2_gb300.se import Common_NL_SE
+    f = synthetic.smoothed_noise_u8((2048, 2048), 1, 4.0)
+    x = dev(f)
+    for maxima in (False, True):
+        out = torch.empty(x.shape, dtype=torch.int64, device="cuda")
+        n = (label.label_maxima if maxima else label.label_minima)(x, Common_NL_SE.SESquare2D, out)
+        exp, m = oracle.label_extrema(f, "SESquare2D", maxima)
+        assert n == m and n > 100
+        np.testing.assert_array_equal(host(out), exp)
 
 
 def test_labelling_rejects_like_the_reference():

@@ -1,5 +1,5 @@
 """The CPU oracle reproduces every known-answer test of the reference's own test-suite
-(test/low_level_morpho/*.cpp, test/geodesy/*.cpp, test/label/label_binary.cpp, label_flat_zones.cpp),
+(test/low_level_morpho/*.cpp, test/geodesy/*.cpp, test/label/label_binary.cpp, label_flat_zones.cpp, label_extrema.cpp),
 before it is trusted as the checker."""
 import numpy as np
 import pytest
@@ -28,6 +28,8 @@ def run_oracle(c):
         return getattr(oracle, op)(ins[0], ins[1], c["se"])
     if op in ("label_binary", "label_flat_zones"):
         return oracle.label(ins[0], c["se"], op == "label_flat_zones")[0]
+    if op in ("label_minima", "label_maxima"):
+        return oracle.label_extrema(ins[0], c["se"], op == "label_maxima")[0]
     raise AssertionError(op)
 
 
@@ -42,7 +44,7 @@ def test_oracle_matches_reference_kat(case):
 def test_kat_count():
     # 20 static + 20 runtime-neighbour-list + 6 line + 4 reconstruction + 6 extrema + 4 leveling
     # + 4 binary labelling + 2 flat-zone labelling
-    assert len(CASES) == 66
+    assert len(CASES) == 68
 
 
 def test_oracle_dilate_y_rejects_non_square():
