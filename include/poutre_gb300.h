@@ -234,6 +234,53 @@ PG_API pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_
 PG_API pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
 PG_API pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
 
+/* ---------------------------------------------------------------- pixel processing */
+/* poutre::CompOpType (include/poutre/base/types.hpp:443-452), same values. */
+typedef enum {
+  PG_COMP_EQUAL = 1,     /* p1 == p2 */
+  PG_COMP_DIFF = 2,      /* p1 != p2 */
+  PG_COMP_SUP = 4,       /* p1 >  p2 */
+  PG_COMP_SUP_EQUAL = 8, /* p1 >= p2 */
+  PG_COMP_INF = 16,      /* p1 <  p2 */
+  PG_COMP_INF_EQUAL = 32 /* p1 <= p2 */
+} pg_comp_op;
+
+/* One operand of CompareImage: an image of the input's geometry (image != NULL) or the scalar
+ * `value` (the reference's ScalarTypeVariant; it must be representable in the operand's pixel
+ * type: integral and in range for integer pixels). */
+typedef struct {
+  const pg_image *image;
+  double value;
+} pg_operand;
+
+/* poutre::ArithInvertImage / ArithSupImage / ArithInfImage / ArithSaturatedAddImage /
+ * ArithSaturatedSubImage (include/poutre/pixel_processing/arith.hpp:31-53): images of one type
+ * and geometry; the output may be one of the inputs (in place), not a partial overlap.  Invert is
+ * -v in the pixel type (wrapping for unsigned pixels); inf / sup are v1 < v2 ? v1 : v2 and
+ * v1 > v2 ? v1 : v2; the saturated sum / difference clamps integers to the type's range and is the
+ * plain IEEE result for floating point, as the reference's vector body computes it (its scalar
+ * remainder loop raises differences below TypeTraits<float>::min() = FLT_MIN, the smallest positive
+ * normal, to FLT_MIN and lowers sums above FLT_MAX to FLT_MAX, so on float images the reference's
+ * last n mod SIMD-width pixels can differ from its others). */
+PG_API pg_status pg_arith_invert_image(const pg_image *in, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_arith_sup_image(const pg_image *in1, const pg_image *in2, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_arith_inf_image(const pg_image *in1, const pg_image *in2, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_sat_add_image(const pg_image *in1, const pg_image *in2, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_sat_sub_image(const pg_image *in1, const pg_image *in2, const pg_image *out, pg_stream_t stream);
+
+/* poutre::CompareImage(i_img, CompOpType, comp, valtrue, valfalse, o_img), all eight overloads
+ * (include/poutre/pixel_processing/compare.hpp:31-84): out = op(in, comp) ? valtrue : valfalse per
+ * pixel.  comp has the input's pixel type, valtrue / valfalse and out the output's (which may
+ * differ from the input's); every image operand has the input's geometry. */
+PG_API pg_status pg_compare_image(const pg_image *in, int32_t op, const pg_operand *comp, const pg_operand *valtrue,
+                                  const pg_operand *valfalse, const pg_image *out, pg_stream_t stream);
+
+/* poutre::CopyInto (same type and geometry) and poutre::ConvertInto (any two pixel types:
+ * static_cast per pixel, defined for values the output type holds; distinct images)
+ * (include/poutre/pixel_processing/copy_convert.hpp, src/pixel_processing/copy_convert.cpp:59,301). */
+PG_API pg_status pg_copy_into(const pg_image *in, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_convert_into(const pg_image *in, const pg_image *out, pg_stream_t stream);
+
 /* ---------------------------------------------------------------- flat morphology adjoint (float32) */
 
 /* Flat dilation (dilate != 0) or erosion by a (2*ry+1) x (2*rx+1) rectangle of `planes` stacked

@@ -240,6 +240,86 @@ inline void label_maxima(const IInterface &i_img, se::Common_NL_SE nl, IInterfac
 }
 }  // namespace label
 
+// ---------------------------------------------------------------- pixel processing
+// poutre::ArithInvertImage / ArithSupImage / ArithInfImage / ArithSaturatedAddImage /
+// ArithSaturatedSubImage / ArithSaturatedAddConstant / ArithSaturatedSubConstant
+// (include/poutre/pixel_processing/arith.hpp:31-53)
+inline void ArithInvertImage(const IInterface &i_img, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_arith_invert_image(&a, &b, o_img.stream()));
+}
+#define PG_FACADE_ARITH2(NAME, FN)                                                 \
+  inline void NAME(const IInterface &i_img1, const IInterface &i_img2, IInterface &o_img) { \
+    pg_image a = i_img1.descriptor(), b = i_img2.descriptor(), c = o_img.descriptor();     \
+    check(FN(&a, &b, &c, o_img.stream()));                                                  \
+  }
+PG_FACADE_ARITH2(ArithSupImage, pg_arith_sup_image)
+PG_FACADE_ARITH2(ArithInfImage, pg_arith_inf_image)
+PG_FACADE_ARITH2(ArithSaturatedAddImage, pg_sat_add_image)
+PG_FACADE_ARITH2(ArithSaturatedSubImage, pg_sat_sub_image)
+#undef PG_FACADE_ARITH2
+inline void ArithSaturatedAddConstant(const IInterface &i_img, double pvalue, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_sat_add_constant(&a, pvalue, &b, o_img.stream()));
+}
+inline void ArithSaturatedSubConstant(const IInterface &i_img, double pvalue, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_sat_sub_constant(&a, pvalue, &b, o_img.stream()));
+}
+
+// poutre::CompOpType (include/poutre/base/types.hpp:443-452)
+enum class CompOpType : int32_t {
+  CompOpUndef = 0,
+  CompOpEqual = PG_COMP_EQUAL,
+  CompOpDiff = PG_COMP_DIFF,
+  CompOpSup = PG_COMP_SUP,
+  CompOpSupEqual = PG_COMP_SUP_EQUAL,
+  CompOpInf = PG_COMP_INF,
+  CompOpInfEqual = PG_COMP_INF_EQUAL
+};
+
+// An operand of CompareImage: an image, or a scalar (the role of ScalarTypeVariant; its value must
+// be representable in the operand's pixel type).  Converts implicitly from either, so the one
+// CompareImage below takes every one of the reference's eight overloads.
+class CompareOperand {
+ public:
+  CompareOperand(const IInterface &img) : img_(&img) {}  // NOLINT(runtime/explicit)
+  CompareOperand(double v) : v_(v) {}                    // NOLINT(runtime/explicit)
+  pg_operand operand(pg_image &storage) const {
+    if (!img_) return pg_operand{nullptr, v_};
+    storage = img_->descriptor();
+    return pg_operand{&storage, 0.0};
+  }
+
+ private:
+  const IInterface *img_ = nullptr;
+  double v_ = 0.0;
+};
+
+// poutre::CompareImage(i_img, compOpType, comp, valtrue, valfalse, o_img)
+// (include/poutre/pixel_processing/compare.hpp:31-84)
+inline void CompareImage(const IInterface &i_img, CompOpType op, const CompareOperand &i_comp,
+                         const CompareOperand &i_valtrue, const CompareOperand &i_valfalse, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), o = o_img.descriptor(), sc, st, sf;
+  const pg_operand c = i_comp.operand(sc), t = i_valtrue.operand(st), f = i_valfalse.operand(sf);
+  check(pg_compare_image(&a, (int32_t)op, &c, &t, &f, &o, o_img.stream()));
+}
+
+// poutre::CopyInto / ConvertInto / Clone (include/poutre/pixel_processing/copy_convert.hpp)
+inline void CopyInto(const IInterface &i_img, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_copy_into(&a, &b, o_img.stream()));
+}
+inline void ConvertInto(const IInterface &i_img, IInterface &o_img) {
+  pg_image a = i_img.descriptor(), b = o_img.descriptor();
+  check(pg_convert_into(&a, &b, o_img.stream()));
+}
+inline DeviceImage Clone(const IInterface &i_img) {
+  DeviceImage o = CloneGeometry(i_img);
+  CopyInto(i_img, o);
+  return o;
+}
+
 // ---------------------------------------------------------------- image strings
 // "Scalar <GUINT8|GUINT16|GINT32|GINT64|F32|D64> <rank> <d0..> <values..>", as poutre's
 // ImageFromString / ImageToString (include/poutre/base/image_interface.hpp:114-122).

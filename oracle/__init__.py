@@ -156,34 +156,83 @@ def _limits(dt):
     return np.iinfo(dt).min, np.iinfo(dt).max
 
 
-def sat_sub_const(img, h):
-    """ArithSaturatedSubConstant (src/pixel_processing/arith.cpp:471; op_Saturated_Sub_Constant
-    arith_op_t.hpp:281-345): result clamped at TypeTraits<T>::min() for integer pixels."""
-    a = _c(img)
+def _saturate(a, b, add: bool):
+    """Saturated a + b / a - b of one pixel type: for integer pixels the exact sum or difference
+    clamped to [TypeTraits<T>::min(), max()] (xsimd's sadd / ssub, which the reference's vector body
+    applies; its scalar remainder loop agrees on every result that is in range of its accumulator),
+    for floating-point pixels the plain IEEE sum or difference of that vector body."""
     if np.issubdtype(a.dtype, np.integer):
         lo, hi = _limits(a.dtype)
-        r = a.astype(np.int64) - int(h)
+        wide = object if a.dtype.itemsize == 8 else np.int64   # exact for 64-bit pixels too
+        r = a.astype(wide) + b.astype(wide) if add else a.astype(wide) - b.astype(wide)
         return np.clip(r, lo, hi).astype(a.dtype)
-    return (a - a.dtype.type(h)).astype(a.dtype)
+    return (a + b if add else a - b).astype(a.dtype)
+
+
+def sat_sub_const(img, h):
+    """ArithSaturatedSubConstant (src/pixel_processing/arith.cpp:471; op_Saturated_Sub_Constant
+    arith_op_t.hpp:281-345)."""
+    a = _c(img)
+    return _saturate(a, np.asarray(h).astype(a.dtype), False)
 
 
 def sat_add_const(img, h):
     """ArithSaturatedAddConstant (op_Saturated_Add_Constant, arith_op_t.hpp:218-276)."""
     a = _c(img)
-    if np.issubdtype(a.dtype, np.integer):
-        lo, hi = _limits(a.dtype)
-        r = a.astype(np.int64) + int(h)
-        return np.clip(r, lo, hi).astype(a.dtype)
-    return (a + a.dtype.type(h)).astype(a.dtype)
+    return _saturate(a, np.asarray(h).astype(a.dtype), True)
 
 
 def sat_sub_image(a, b):
-    """ArithSaturatedSubImage (op_Saturated_Sub, arith_op_t.hpp:84-121)."""
+    """ArithSaturatedSubImage (src/pixel_processing/arith.cpp:195; op_Saturated_Sub arith_op_t.hpp:84-121)."""
+    return _saturate(_c(a), _c(b), False)
+
+
+def sat_add_image(a, b):
+    """ArithSaturatedAddImage (src/pixel_processing/arith.cpp:125; op_Saturated_Add arith_op_t.hpp:146-183)."""
+    return _saturate(_c(a), _c(b), True)
+
+
+def sup_image(a, b):
+    """ArithSupImage (op_Sup arith_op_t.hpp:346-366): a > b ? a : b."""
     a = _c(a); b = _c(b)
-    if np.issubdtype(a.dtype, np.integer):
-        lo, hi = _limits(a.dtype)
-        return np.clip(a.astype(np.int64) - b.astype(np.int64), lo, hi).astype(a.dtype)
-    return (a - b).astype(a.dtype)
+    return np.where(a > b, a, b).astype(a.dtype)
+
+
+def inf_image(a, b):
+    """ArithInfImage (op_Inf arith_op_t.hpp:396-417): a < b ? a : b."""
+    a = _c(a); b = _c(b)
+    return np.where(a < b, a, b).astype(a.dtype)
+
+
+def invert_image(a):
+    """ArithInvertImage (op_Invert arith_op_t.hpp:40-58): -a in the pixel type (wraps for unsigned
+    and for the most negative signed value)."""
+    a = _c(a)
+    with np.errstate(over="ignore"):
+        return np.negative(a).astype(a.dtype)
+
+
+COMPARE_OPS = {"equal": np.equal, "diff": np.not_equal, "sup": np.greater, "sup_equal": np.greater_equal,
+               "inf": np.less, "inf_equal": np.less_equal}
+
+
+def compare(img, op: str, comp, valtrue, valfalse, out_dtype):
+    """CompareImage (include/poutre/pixel_processing/compare.hpp:31-84; OpComp* compare_op_t.hpp:41-165):
+    out = op(img, comp) ? valtrue : valfalse.  comp (a scalar or an image) has the input's type,
+    valtrue / valfalse (scalars or images) the output's."""
+    a = _c(img)
+    od = np.dtype(out_dtype)
+    c = np.asarray(comp).astype(a.dtype)
+    t = np.asarray(valtrue).astype(od)
+    f = np.asarray(valfalse).astype(od)
+    return np.where(COMPARE_OPS[op](a, c), t, f).astype(od)
+
+
+def convert(img, out_dtype):
+    """ConvertInto (src/pixel_processing/copy_convert.cpp:301; CopyOpDispatcher copy_convert_t.hpp:33-86):
+    static_cast of every pixel (truncation toward zero from floating point, modular narrowing of
+    integers, round-to-nearest into floating point); defined for values the target type holds."""
+    return _c(img).astype(np.dtype(out_dtype))
 
 
 def lowest(dt):

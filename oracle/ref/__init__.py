@@ -45,6 +45,10 @@ def lib():
             L.ref_label.argtypes = [I, I, I, P, P, P, I, P]
         if hasattr(L, "ref_label_extrema"):
             L.ref_label_extrema.argtypes = [I, I, I, P, P, P, I]
+        if hasattr(L, "ref_arith"):
+            L.ref_arith.argtypes = [I, I, I, P, P, P, P]
+            L.ref_compare.argtypes = [I, I, I, P, P, I, P, P, P]
+            L.ref_convert.argtypes = [I, I, I, P, P, P]
         _lib = L
     return _lib
 
@@ -124,4 +128,43 @@ def label_extrema(img, se="SESquare2D", maxima=False):
     a = np.ascontiguousarray(img)
     out = np.empty(a.shape, dtype=np.int64)
     _chk(lib().ref_label_extrema(int(maxima), PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out), SE[se]))
+    return out
+
+
+ARITH = {"invert": 0, "sup": 1, "inf": 2, "sat_add": 3, "sat_sub": 4}
+
+
+def arith(kind, a, b=None):
+    """ArithInvert/Sup/Inf/SaturatedAdd/SaturatedSub image on the compiled reference."""
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(a if b is None else b)
+    out = np.empty_like(a)
+    _chk(lib().ref_arith(ARITH[kind], PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(b), _p(out)))
+    return out
+
+
+COMP = {"equal": 1, "diff": 2, "sup": 4, "sup_equal": 8, "inf": 16, "inf_equal": 32}
+
+
+def compare(img, op, comp, valtrue, valfalse, out_dtype):
+    """CompareImage on the compiled reference; each operand an ndarray (image) or a number (scalar)."""
+    a = np.ascontiguousarray(img)
+    od = np.dtype(out_dtype)
+    out = np.empty(a.shape, dtype=od)
+    keep, ptrs, vals = [], (ctypes.c_void_p * 3)(), (ctypes.c_double * 3)()
+    for k, (v, dt) in enumerate(((comp, a.dtype), (valtrue, od), (valfalse, od))):
+        if isinstance(v, np.ndarray):
+            v = np.ascontiguousarray(v, dtype=dt)
+            keep.append(v)
+            ptrs[k] = v.ctypes.data
+        else:
+            vals[k] = float(v)
+    _chk(lib().ref_compare(PTYPE[a.dtype], PTYPE[od], a.ndim, _shape(a), _p(a), COMP[op], ptrs, vals, _p(out)))
+    return out
+
+
+def convert(img, out_dtype):
+    a = np.ascontiguousarray(img)
+    out = np.empty(a.shape, dtype=np.dtype(out_dtype))
+    _chk(lib().ref_convert(PTYPE[a.dtype], PTYPE[out.dtype], a.ndim, _shape(a), _p(a), _p(out)))
     return out

@@ -16,7 +16,9 @@
 #include <poutre/label/label_flat_zones.hpp>
 #include <poutre/low_level_morpho/ero_dil.hpp>
 #include <poutre/low_level_morpho/ero_dil_line.hpp>
+#include <poutre/pixel_processing/arith.hpp>
 #include <poutre/pixel_processing/compare.hpp>
+#include <poutre/pixel_processing/copy_convert.hpp>
 #include <poutre/structuring_element/details/neighbor_list_se_t.hpp>
 
 #include <cstdint>
@@ -206,6 +208,65 @@ int ref_label(int flat, int pt, int rank, const int64_t *shape, const void *in, 
     const std::size_t c = flat ? poutre::label::label_flat_zones(*a, s, *o) : poutre::label::label_binary(*a, s, *o);
     take(*o, 32, rank, shape, out);
     *n = static_cast<int64_t>(c);
+  });
+}
+
+// poutre::ArithInvertImage (kind 0), ArithSupImage (1), ArithInfImage (2), ArithSaturatedAddImage (3),
+// ArithSaturatedSubImage (4), include/poutre/pixel_processing/arith.hpp:31-53
+int ref_arith(int kind, int pt, int rank, const int64_t *shape, const void *a, const void *b, void *out) {
+  return guarded([&] {
+    auto x = make(pt, rank, shape, a);
+    auto y = make(pt, rank, shape, b);
+    auto o = make(pt, rank, shape, nullptr);
+    switch (kind) {
+      case 0: poutre::ArithInvertImage(*x, *o); break;
+      case 1: poutre::ArithSupImage(*x, *y, *o); break;
+      case 2: poutre::ArithInfImage(*x, *y, *o); break;
+      case 3: poutre::ArithSaturatedAddImage(*x, *y, *o); break;
+      case 4: poutre::ArithSaturatedSubImage(*x, *y, *o); break;
+      default: throw std::runtime_error("harness: arith kind");
+    }
+    take(*o, pt, rank, shape, out);
+  });
+}
+
+// poutre::CompareImage, the overload chosen per operand: image k when imgs[k] != nullptr, else the
+// scalar vals[k] (k = comparand, true value, false value), include/poutre/pixel_processing/compare.hpp:31-84
+int ref_compare(int pt_in, int pt_out, int rank, const int64_t *shape, const void *in, int op,
+                const void *const *imgs, const double *vals, void *out) {
+  return guarded([&] {
+    auto x = make(pt_in, rank, shape, in);
+    auto o = make(pt_out, rank, shape, nullptr);
+    std::unique_ptr<poutre::IInterface> im[3];
+    poutre::ScalarTypeVariant sc[3];
+    for (int k = 0; k < 3; ++k) {
+      const int pt = k == 0 ? pt_in : pt_out;
+      if (imgs[k]) im[k] = make(pt, rank, shape, imgs[k]);
+      else sc[k] = scalar_of(pt, vals[k]);
+    }
+    const auto c = static_cast<poutre::CompOpType>(op);
+    const int form = (im[0] ? 4 : 0) | (im[1] ? 2 : 0) | (im[2] ? 1 : 0);
+    switch (form) {
+      case 0: poutre::CompareImage(*x, c, sc[0], sc[1], sc[2], *o); break;
+      case 1: poutre::CompareImage(*x, c, sc[0], sc[1], *im[2], *o); break;
+      case 2: poutre::CompareImage(*x, c, sc[0], *im[1], sc[2], *o); break;
+      case 3: poutre::CompareImage(*x, c, sc[0], *im[1], *im[2], *o); break;
+      case 4: poutre::CompareImage(*x, c, *im[0], sc[1], sc[2], *o); break;
+      case 5: poutre::CompareImage(*x, c, *im[0], sc[1], *im[2], *o); break;
+      case 6: poutre::CompareImage(*x, c, *im[0], *im[1], sc[2], *o); break;
+      default: poutre::CompareImage(*x, c, *im[0], *im[1], *im[2], *o); break;
+    }
+    take(*o, pt_out, rank, shape, out);
+  });
+}
+
+// poutre::ConvertInto, src/pixel_processing/copy_convert.cpp:301
+int ref_convert(int pt_in, int pt_out, int rank, const int64_t *shape, const void *in, void *out) {
+  return guarded([&] {
+    auto x = make(pt_in, rank, shape, in);
+    auto o = make(pt_out, rank, shape, nullptr);
+    poutre::ConvertInto(*x, *o);
+    take(*o, pt_out, rank, shape, out);
   });
 }
 

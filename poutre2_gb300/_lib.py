@@ -30,6 +30,8 @@ EXPORTED = [
     "pg_dynamic_pseudo_opening", "pg_dynamic_pseudo_closing", "pg_h_maxima_binary", "pg_h_maxima_binary_batch",
     "pg_low_leveling", "pg_high_leveling", "pg_leveling",
     "pg_sat_sub_constant", "pg_sat_add_constant",
+    "pg_arith_invert_image", "pg_arith_sup_image", "pg_arith_inf_image", "pg_sat_add_image", "pg_sat_sub_image",
+    "pg_compare_image", "pg_copy_into", "pg_convert_into",
     "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
     "pg_check_device", "pg_last_reconstruction_rounds", "pg_reconstruction_noalloc",
     "pg_h_maxima_binary_batch_plan", "pg_batch_plan_run", "pg_batch_plan_config", "pg_batch_plan_set_config",
@@ -48,6 +50,11 @@ class PoutreError(RuntimeError):
 class PgImage(ctypes.Structure):
     _fields_ = [("data", ctypes.c_void_p), ("ptype", ctypes.c_int32), ("rank", ctypes.c_int32),
                 ("shape", ctypes.c_int64 * 3)]
+
+
+class PgOperand(ctypes.Structure):
+    """pg_operand: an image (``image`` set) or the scalar ``value`` of CompareImage."""
+    _fields_ = [("image", ctypes.POINTER(PgImage)), ("value", ctypes.c_double)]
 
 
 class PgSE(ctypes.Structure):
@@ -96,6 +103,12 @@ def load(path: str | None = None):
             "pg_low_leveling": [img, img, I32, img, VP], "pg_high_leveling": [img, img, I32, img, VP],
             "pg_leveling": [img, img, I32, img, VP],
             "pg_sat_sub_constant": [img, D, img, VP], "pg_sat_add_constant": [img, D, img, VP],
+            "pg_arith_invert_image": [img, img, VP], "pg_arith_sup_image": [img, img, img, VP],
+            "pg_arith_inf_image": [img, img, img, VP], "pg_sat_add_image": [img, img, img, VP],
+            "pg_sat_sub_image": [img, img, img, VP],
+            "pg_compare_image": [img, I32, ctypes.POINTER(PgOperand), ctypes.POINTER(PgOperand),
+                                 ctypes.POINTER(PgOperand), img, VP],
+            "pg_copy_into": [img, img, VP], "pg_convert_into": [img, img, VP],
             "pg_flat_morph2d_forward": [fp, fp, I64, I64, I64, I32, I32, I32, VP],
             "pg_flat_morph2d_backward": [fp, fp, fp, I64, I64, I64, I32, I32, I32, VP],
             "pg_check_device": [VP],

@@ -647,6 +647,99 @@ pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out,
   return launch_sat_const(*in, v, true, *out, STREAM(s));
 }
 
+// ---------------------------------------------------------------- pixel processing
+// An output may be exactly one of the inputs (same buffer, same pixel size: every pixel is read
+// before it is written, by one thread) but may not overlap one partially.
+static bool partial_overlap(const pg_image &a, const pg_image &b) {
+  return overlaps(a, b) && !(a.data == b.data && elem_size(a.ptype) == elem_size(b.ptype));
+}
+
+// src/pixel_processing/arith.cpp:125-300: AssertSizesCompatible / AssertAsTypesCompatible on every pair
+static pg_status pixel_arith(const pg_image *a, const pg_image *b, const pg_image *out, int op, const char *what,
+                             cudaStream_t s) {
+  PG_TRY(check_image(a, what));
+  if (b) PG_TRY(check_image(b, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*a, *out) || (b && !same_geometry(*b, *out)))
+    return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images have not compatible sizes");
+  if (a->ptype != out->ptype || (b && b->ptype != out->ptype))
+    return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images must have compatible types");
+  if (partial_overlap(*a, *out) || (b && partial_overlap(*b, *out)))
+    return fail(PG_ERR_ALIASING, std::string(what) + " output overlaps an input partially");
+  return launch_pixel_arith(op, *a, b, *out, s);
+}
+
+pg_status pg_arith_invert_image(const pg_image *in, const pg_image *out, pg_stream_t s) {
+  return pixel_arith(in, nullptr, out, PX_NEG, "ArithInvertImage", STREAM(s));
+}
+pg_status pg_arith_sup_image(const pg_image *a, const pg_image *b, const pg_image *out, pg_stream_t s) {
+  return pixel_arith(a, b, out, PX_SUP, "ArithSupImage", STREAM(s));
+}
+pg_status pg_arith_inf_image(const pg_image *a, const pg_image *b, const pg_image *out, pg_stream_t s) {
+  return pixel_arith(a, b, out, PX_INF, "ArithInfImage", STREAM(s));
+}
+pg_status pg_sat_add_image(const pg_image *a, const pg_image *b, const pg_image *out, pg_stream_t s) {
+  return pixel_arith(a, b, out, PX_SADD, "ArithSaturatedAddImage", STREAM(s));
+}
+pg_status pg_sat_sub_image(const pg_image *a, const pg_image *b, const pg_image *out, pg_stream_t s) {
+  return pixel_arith(a, b, out, PX_SSUB, "ArithSaturatedSubImage", STREAM(s));
+}
+
+// src/pixel_processing/compare.cpp:601-1000: sizes of every image compatible with the output; the
+// comparand has the input's type, the true / false values the output's (std::get<pType> on a
+// scalar, a downcast on an image, both throwing otherwise)
+pg_status pg_compare_image(const pg_image *in, int32_t op, const pg_operand *comp, const pg_operand *valtrue,
+                           const pg_operand *valfalse, const pg_image *out, pg_stream_t s) {
+  const char *what = "CompareImage";
+  PG_TRY(check_image(in, what));
+  PG_TRY(check_image(out, what));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, "CompareImage images have not compatible sizes");
+  switch (op) {
+    case PG_COMP_EQUAL: case PG_COMP_DIFF: case PG_COMP_SUP: case PG_COMP_SUP_EQUAL: case PG_COMP_INF:
+    case PG_COMP_INF_EQUAL: break;
+    default: return fail(PG_ERR_INVALID_ARGUMENT, "CompareImage unsupported CompOpType");
+  }
+  if (!comp || !valtrue || !valfalse) return fail(PG_ERR_INVALID_ARGUMENT, "CompareImage: null operand");
+  if (partial_overlap(*in, *out)) return fail(PG_ERR_ALIASING, "CompareImage output overlaps an input partially");
+  const pg_operand *src[3] = {comp, valtrue, valfalse};
+  static const char *names[3] = {"i_comp", "i_valtrue", "i_valfalse"};
+  CompareOperand ops[3];
+  for (int k = 0; k < 3; ++k) {
+    const int pt = k == 0 ? in->ptype : out->ptype;
+    const pg_image *im = src[k]->image;
+    if (im) {
+      PG_TRY(check_image(im, what));
+      if (!same_geometry(*im, *out)) return fail(PG_ERR_INCOMPATIBLE, "CompareImage images have not compatible sizes");
+      if (im->ptype != pt) return fail(PG_ERR_INCOMPATIBLE, std::string("CompareImage ") + names[k] + " downcast fail");
+      if (partial_overlap(*im, *out)) return fail(PG_ERR_ALIASING, "CompareImage output overlaps an input partially");
+      ops[k] = CompareOperand{im->data, 0.0};
+    } else {
+      PG_TRY(check_scalar(pt, src[k]->value,
+                          (std::string("CompareImage unable to extract suitable type from ") + names[k]).c_str()));
+      ops[k] = CompareOperand{nullptr, src[k]->value};
+    }
+  }
+  return launch_compare(*in, op, ops[0], ops[1], ops[2], *out, STREAM(s));
+}
+
+// src/pixel_processing/copy_convert.cpp:59-67, :301-306
+pg_status pg_copy_into(const pg_image *in, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_image(in, "CopyInto"));
+  PG_TRY(check_image(out, "CopyInto"));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, "Copy images have not compatible sizes");
+  if (in->ptype != out->ptype) return fail(PG_ERR_INCOMPATIBLE, "Copy images have not compatible types");
+  if (in->data == out->data) return PG_OK;
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, "Copy images overlap partially");
+  return launch_copy(*in, *out, STREAM(s));
+}
+pg_status pg_convert_into(const pg_image *in, const pg_image *out, pg_stream_t s) {
+  PG_TRY(check_image(in, "ConvertInto"));
+  PG_TRY(check_image(out, "ConvertInto"));
+  if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, "ConvertInto images have not compatible sizes");
+  if (overlaps(*in, *out)) return fail(PG_ERR_ALIASING, "ConvertInto images must be differents");
+  return launch_convert(*in, *out, STREAM(s));
+}
+
 // ---------------------------------------------------------------- adjoint
 pg_status pg_flat_morph2d_forward(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int32_t ry,
                                   int32_t rx, int32_t dilate, pg_stream_t s) {

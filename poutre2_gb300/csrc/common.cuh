@@ -25,6 +25,33 @@ template <> struct Lim<float>    { __host__ __device__ static constexpr float lo
 template <> struct Lim<double>   { __host__ __device__ static constexpr double lo() { return -DBL_MAX; }    __host__ __device__ static constexpr double hi() { return DBL_MAX; } };
 
 // read-only cached load for every pixel type (8-byte integers through long long)
+// saturating a - v and a + v: integers clamped to the pixel type's range (TypeTraits<T>::min/max,
+// xsimd's ssub / sadd), floating point the plain IEEE result
+template <typename T>
+__host__ __device__ __forceinline__ T sat_sub_c(T a, T v) {
+  if constexpr (std::is_integral_v<T>) {
+    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
+    const Wide r = (Wide)a - (Wide)v;
+    if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
+    if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
+    return (T)r;
+  } else {
+    return a - v;
+  }
+}
+template <typename T>
+__host__ __device__ __forceinline__ T sat_add_c(T a, T v) {
+  if constexpr (std::is_integral_v<T>) {
+    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
+    const Wide r = (Wide)a + (Wide)v;
+    if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
+    if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
+    return (T)r;
+  } else {
+    return a + v;
+  }
+}
+
 template <typename T> __device__ __forceinline__ T ldg(const T *p) {
   if constexpr (std::is_same_v<T, int64_t>) return (T)__ldg(reinterpret_cast<const long long *>(p));
   else return __ldg(p);
@@ -210,6 +237,17 @@ pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
 pg_status launch_sat_const(const pg_image &in, double v, bool add, const pg_image &out, cudaStream_t s);
 pg_status launch_sat_sub_image(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
+
+// pixel.cu: ArithInf/Sup/SaturatedAdd/SaturatedSub/Invert image, CompareImage, ConvertInto
+enum PixelOp { PX_INF = 0, PX_SUP = 1, PX_SADD = 2, PX_SSUB = 3, PX_NEG = 4 };
+pg_status launch_pixel_arith(int op, const pg_image &a, const pg_image *b, const pg_image &out, cudaStream_t s);
+struct CompareOperand {
+  const void *data;  // image pixels, or nullptr for the scalar `value`
+  double value;
+};
+pg_status launch_compare(const pg_image &in, int op, const CompareOperand &comp, const CompareOperand &vt,
+                         const CompareOperand &vf, const pg_image &out, cudaStream_t s);
+pg_status launch_convert(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_dyn_pseudo_marker(const pg_image &f, const pg_image &ext, double h, bool opening, const pg_image &out,
                                    cudaStream_t s);
 

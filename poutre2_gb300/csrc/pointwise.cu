@@ -19,32 +19,6 @@ static unsigned grid_for(int64_t n, int threads = 256) {
   return (unsigned)b;
 }
 
-// saturating a - v and a + v, clamped to the pixel type's range (TypeTraits<T>::min/max)
-template <typename T>
-__host__ __device__ __forceinline__ T sat_sub_c(T a, T v) {
-  if constexpr (std::is_integral_v<T>) {
-    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
-    const Wide r = (Wide)a - (Wide)v;
-    if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
-    if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
-    return (T)r;
-  } else {
-    return a - v;
-  }
-}
-template <typename T>
-__host__ __device__ __forceinline__ T sat_add_c(T a, T v) {
-  if constexpr (std::is_integral_v<T>) {
-    using Wide = std::conditional_t<(sizeof(T) < 8), long long, __int128>;
-    const Wide r = (Wide)a + (Wide)v;
-    if (r > (Wide)Lim<T>::hi()) return Lim<T>::hi();
-    if (r < (Wide)Lim<T>::lo()) return Lim<T>::lo();
-    return (T)r;
-  } else {
-    return a + v;
-  }
-}
-
 template <typename T>
 __global__ void k_sat_const(const T *__restrict__ in, T *__restrict__ out, int64_t n, T v, bool add) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {

@@ -3,7 +3,9 @@
 // with ImageFromString, call the poutre-named entry point, compare ImageToString.
 //
 // Usage: facade_test <cases file>; one case per line, fields separated by ';':
-//   op;se;param;input1;input2;expected     (input2 empty for one-input operators)
+//   op;se;param;expected;input1[;input2;...]
+// For "compare" cases se is the CompOpType name and param lists the comparand, true and false
+// operands as '|'-separated tokens: "#k" for input image k, a number for a scalar.
 // Exit status: number of failed cases (0 = all pass).
 #include <fstream>
 #include <iostream>
@@ -71,12 +73,12 @@ int main(int argc, char **argv) {
   while (std::getline(f, line)) {
     if (line.empty()) continue;
     auto v = split(line, ';');
-    if (v.size() != 6) { std::cerr << "bad case line\n"; return 101; }
-    const std::string &op = v[0], &sen = v[1];
-    const double param = v[2].empty() ? 0.0 : std::stod(v[2]);
+    if (v.size() < 5) { std::cerr << "bad case line\n"; return 101; }
+    const std::string &op = v[0], &sen = v[1], &expected = v[3];
+    const double param = v[2].empty() || op == "compare" ? 0.0 : std::stod(v[2]);
     try {
-      DeviceImage a = ImageFromString(v[3]);
-      DeviceImage o = CloneGeometry(a);
+      DeviceImage a = ImageFromString(v[4]);
+      DeviceImage o = op == "compare" ? CloneGeometry(ImageFromString(expected)) : CloneGeometry(a);
       if (op == "dilate_static") Dilate(a, se_of(sen), 1, o);
       else if (op == "erode_static") Erode(a, se_of(sen), 1, o);
       else if (op == "dilate_nl") Dilate(a, nl_of(sen), o);
@@ -86,11 +88,11 @@ int main(int argc, char **argv) {
       else if (op == "dilatey") DilateY(a, (std::ptrdiff_t)param, o);
       else if (op == "erodey") ErodeY(a, (std::ptrdiff_t)param, o);
       else if (op == "reconstruct_dilate" || op == "reconstruct_erode") {
-        DeviceImage b = ImageFromString(v[4]);
+        DeviceImage b = ImageFromString(v[5]);
         geo::Reconstruction(op == "reconstruct_dilate" ? geo::reconstruction_type::dilate : geo::reconstruction_type::erode,
                             a, b, se_of(sen), o);
       } else if (op == "low_leveling" || op == "high_leveling" || op == "leveling") {
-        DeviceImage b = ImageFromString(v[4]);
+        DeviceImage b = ImageFromString(v[5]);
         if (op == "low_leveling") geo::low_leveling(a, b, se_of(sen), o);
         else if (op == "high_leveling") geo::high_leveling(a, b, se_of(sen), o);
         else geo::leveling(a, b, se_of(sen), o);
@@ -104,12 +106,26 @@ int main(int argc, char **argv) {
       else if (op == "label_flat_zones") label::label_flat_zones(a, se_of(sen), o);
       else if (op == "label_minima") label::label_minima(a, se_of(sen), o);
       else if (op == "label_maxima") label::label_maxima(a, se_of(sen), o);
+      else if (op == "compare") {
+        std::vector<DeviceImage> ins;
+        for (std::size_t k = 5; k < v.size(); ++k) ins.push_back(ImageFromString(v[k]));
+        const auto tok = split(v[2], '|');
+        auto opnd = [&](const std::string &t) -> CompareOperand {
+          if (t[0] == '#') return CompareOperand(std::stoi(t.substr(1)) == 0 ? (const IInterface &)a : ins.at(std::stoi(t.substr(1)) - 1));
+          return CompareOperand(std::stod(t));
+        };
+        static const std::map<std::string, CompOpType> ops = {
+            {"equal", CompOpType::CompOpEqual}, {"diff", CompOpType::CompOpDiff}, {"sup", CompOpType::CompOpSup},
+            {"sup_equal", CompOpType::CompOpSupEqual}, {"inf", CompOpType::CompOpInf},
+            {"inf_equal", CompOpType::CompOpInfEqual}};
+        CompareImage(a, ops.at(sen), opnd(tok.at(0)), opnd(tok.at(1)), opnd(tok.at(2)), o);
+      }
       else { std::cerr << "unknown op " << op << "\n"; return 102; }
       ++run;
       const std::string got = ImageToString(o);
-      if (got != v[5]) {
+      if (got != expected) {
         ++failed;
-        std::cerr << "FAIL " << op << " " << sen << "\n  got      " << got << "\n  expected " << v[5] << "\n";
+        std::cerr << "FAIL " << op << " " << sen << "\n  got      " << got << "\n  expected " << expected << "\n";
       }
     } catch (const std::exception &e) {
       ++failed;

@@ -122,12 +122,74 @@ def extract(root: str):
     return cases
 
 
+# poutre2's compare tests (test/pixel_processing/compare.cpp) call the template layer
+# (t_CompareImage_xyz / ViewCompare_xyz_func_helper) on images built by ImageFromString, named
+# scalars (`const poutre::pINT32 valcomp = 5;`) and literals; x, y, z say whether the comparand,
+# the true value and the false value are a scalar (s) or an image (i).  Cases on sections of an
+# image are skipped.
+COMP_OPS = {"CompOpEqual": "equal", "CompOpDiff": "diff", "CompOpSup": "sup", "CompOpSupEqual": "sup_equal",
+            "CompOpInf": "inf", "CompOpInfEqual": "inf_equal"}
+COMPARE_FILE = "test/pixel_processing/compare.cpp"
+
+
+def _string_literal(text: str, start: int):
+    m = re.compile(r'"((?:[^"\\]|\\.|\\\n)*)"', re.S).search(text, start)
+    return m.group(1), m.end()
+
+
+def extract_compare(root: str):
+    text = open(os.path.join(root, COMPARE_FILE)).read()
+    starts = [m.start() for m in re.finditer(r"TEST_CASE\s*\(", text)] + [len(text)]
+    cases = []
+    for a, b in zip(starts, starts[1:]):
+        body = text[a:b]
+        name = re.match(r'TEST_CASE\s*\(\s*"([^"]*)"', body).group(1)
+        call = re.search(r"(?:t_CompareImage_|ViewCompare_)(?P<form>[si]{3})\w*\((?P<args>[^;]*)\)\s*;", body)
+        if call is None or "section" in body:
+            continue
+        images, alias, scalars = {}, {}, {}
+        for m in re.finditer(r"(?:const\s+)?auto\s+(\w+)\s*=\s*poutre::ImageFromString\(", body):
+            lit, _ = _string_literal(body, m.end())
+            images[m.group(1)] = parse_image(lit)
+        for m in re.finditer(r"(?:const\s+)?auto\s*\*?\s*(\w+)\s*=\s*dynamic_cast<[^>]*>\((\w+)\.get\(\)\)", body):
+            alias[m.group(1)] = m.group(2)
+        for m in re.finditer(r"auto\s+(\w+)\s*=\s*poutre::details::view\(\*?(\w+)\)", body):
+            alias[m.group(1)] = m.group(2)
+        for m in re.finditer(r"const\s+poutre::p\w+\s+(\w+)\s*=\s*(-?[\d.]+)\s*;", body):
+            scalars[m.group(1)] = m.group(2)
+        out = re.search(r"image_t<poutre::(p\w+)>\s+imgout", body).group(1)
+
+        def resolve(tok):
+            tok = tok.strip().lstrip("*")
+            while tok in alias:
+                tok = alias[tok]
+            return tok
+
+        args = [re.sub(r"//\S*", "", x).strip() for x in call.group("args").split(",")]
+        op = COMP_OPS[args[1].split("::")[-1]]
+        src = resolve(args[0])
+        inputs = [images[src]]
+        operands = []
+        for kind, tok in zip(call.group("form"), args[2:5]):
+            if kind == "s":
+                v = scalars.get(tok, tok)
+                operands.append({"scalar": float(v) if "." in v else int(v)})
+            else:
+                inputs.append(images[resolve(tok)])
+                operands.append({"image": len(inputs) - 1})
+        lit, _ = _string_literal(body, body.index("expected", call.end()))
+        cases.append({"name": name, "file": COMPARE_FILE, "line": text.count("\n", 0, a + call.start()) + 1,
+                      "op": "compare", "cmp": op, "form": call.group("form"), "operands": operands,
+                      "out_ptype": out, "inputs": inputs, "expected": parse_image(lit)})
+    return cases
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    cases = extract(root)
+    cases = extract(root) + extract_compare(root)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(out, "w") as f:
-        json.dump({"source": "poutre2 Catch2 tests (test/low_level_morpho, test/geodesy, test/label)", "cases": cases},
+        json.dump({"source": "poutre2 Catch2 tests (test/low_level_morpho, test/geodesy, test/label, test/pixel_processing/compare.cpp)", "cases": cases},
                   f, indent=1)
     print(f"wrote {len(cases)} cases to {out}")
 

@@ -118,3 +118,62 @@ def test_labelling_argument_checks_need_no_gpu(lib_path):
         assert fn(ctypes.byref(a), 2, ctypes.byref(a), ctypes.byref(n), None) == 5  # in place
         assert fn(ctypes.byref(a), 9, ctypes.byref(o), ctypes.byref(n), None) == 3  # 3D SE, 2D image
         assert fn(ctypes.byref(af), 2, ctypes.byref(o), ctypes.byref(n), None) == 2  # float image
+
+
+def test_pixel_processing_argument_checks_need_no_gpu(lib_path):
+    # types, sizes, partial overlaps, CompOpType values and scalar ranges are rejected before any
+    # device work, as the reference's asserts and std::get<pType> would
+    import ctypes
+    from poutre2_gb300 import _lib
+    L = _lib.load()
+
+    def img(ptype, shape, data):
+        d = _lib.PgImage()
+        d.data, d.ptype, d.rank = data, ptype, len(shape)
+        for i, s in enumerate(shape):
+            d.shape[i] = s
+        return d
+
+    a, b = img(8, (8, 8), 0x10000), img(8, (8, 8), 0x20000)
+    o = img(8, (8, 8), 0x30000)
+    wide = img(32, (8, 8), 0x30000)
+    B = ctypes.byref
+    assert L.pg_arith_sup_image(B(a), B(img(32, (8, 8), 0x20000)), B(o), None) == 4   # types differ
+    assert L.pg_sat_add_image(B(a), B(img(8, (8, 9), 0x20000)), B(o), None) == 4      # sizes differ
+    assert L.pg_arith_inf_image(B(a), B(b), B(img(8, (8, 8), 0x10000 + 12)), None) == 5  # partial overlap
+    assert L.pg_arith_invert_image(B(a), B(img(8, (8, 8), 0x10004)), None) == 5
+    assert L.pg_convert_into(B(a), B(img(16, (8, 8), 0x10000)), None) == 5            # must be different
+    assert L.pg_copy_into(B(a), B(wide), None) == 4
+    s = lambda v: _lib.PgOperand(None, v)  # noqa: E731
+    i = lambda d: _lib.PgOperand(ctypes.pointer(d), 0.0)  # noqa: E731
+    assert L.pg_compare_image(B(a), 3, B(s(1)), B(s(1)), B(s(0)), B(o), None) == 1     # not a CompOpType
+    assert L.pg_compare_image(B(a), 4, B(s(0.5)), B(s(1)), B(s(0)), B(o), None) == 1   # 0.5 is no INT32
+    assert L.pg_compare_image(B(a), 4, B(s(1)), B(s(300)), B(s(0)),
+                              B(img(4, (8, 8), 0x30000)), None) == 1                    # 300 is no UINT8
+    assert L.pg_compare_image(B(a), 4, B(i(img(32, (8, 8), 0x20000))), B(s(1)), B(s(0)), B(o), None) == 4
+    assert L.pg_compare_image(B(a), 4, B(s(1)), B(i(img(8, (8, 8), 0x20000))), B(s(0)), B(wide), None) == 4
+    assert L.pg_compare_image(B(a), 4, B(s(1)), B(s(1)), B(s(0)), B(img(8, (4, 16), 0x30000)), None) == 4
+
+
+# pypoutre's function and enum names (python/*/*.cpp of poutre2), all present in the mirror
+PYPOUTRE_NAMES = [
+    "PType", "CType", "Comp", "Image", "as_sizes_compatible", "as_types_compatible", "are_images_different",
+    "factory_image", "from_string", "to_string", "arith_invert_image", "arith_inf_image", "arith_sup_image",
+    "arith_saturated_add_image", "arith_saturated_sub_image", "arith_saturated_add_constant",
+    "arith_saturated_sub_constant", "compare", "clone", "clone_geometry", "convert", "convert_geometry",
+    "copy_into", "convert_into", "se_type", "static_nl_se", "static_compound_se", "erode", "dilate", "dilateX",
+    "dilateY", "erodeX", "erodeY", "RecType", "h_minima", "h_maxima", "h_concave", "h_convex",
+    "dynamic_pseudo_closing", "dynamic_pseudo_opening", "high_leveling", "low_leveling", "leveling",
+    "label_binary", "label_flat_zones", "label_maxima", "label_minima"]
+
+
+def test_pypoutre_mirror_names_and_enums():
+    from poutre2_gb300 import pypoutre as pp
+    for name in PYPOUTRE_NAMES:
+        assert hasattr(pp, name), name
+    assert [m.name for m in pp.static_nl_se] == ["segx1d", "square2d", "cross2d", "segx2d", "segy2d", "segx3d",
+                                                 "segy3d", "segz3d", "cross3d", "square3d"]
+    assert {m.name for m in pp.Comp} == {"Diff", "Equal", "Inf", "Sup", "InfEqual", "SupEqual"}
+    assert int(pp.Comp.Sup) == 4 and int(pp.PType.GrayUINT8) == 4 and int(pp.RecType.dilate) == 1
+    with pytest.raises(Exception):
+        pp.Image(__import__("torch").zeros(3, 3))  # a host tensor is no device image

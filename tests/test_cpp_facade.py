@@ -41,12 +41,15 @@ def test_facade_replays_reference_kats(tmp_path):
     _compile(exe)
     lines = []
     for c in load_cases():
-        param = c.get("half", c.get("h", ""))
-        ins = [_img(i) for i in c["inputs"]] + [""]
-        lines.append(";".join([c["op"], c.get("se") or "", "" if param is None else str(param), ins[0], ins[1],
-                               _img(c["expected"])]))
+        if c["op"] == "compare":
+            se = c["cmp"]
+            param = "|".join(f"#{o['image']}" if "image" in o else str(o["scalar"]) for o in c["operands"])
+        else:
+            se, param = c.get("se") or "", c.get("half", c.get("h", ""))
+        lines.append(";".join([c["op"], se, "" if param is None else str(param), _img(c["expected"])]
+                              + [_img(i) for i in c["inputs"]]))
     cases = tmp_path / "cases.txt"
     cases.write_text("\n".join(lines) + "\n")
     r = subprocess.run([exe, str(cases)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "68 cases, 0 failed" in r.stdout
+    assert "116 cases, 0 failed" in r.stdout

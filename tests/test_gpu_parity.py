@@ -64,6 +64,11 @@ def test_reference_kat_on_gpu(case):
                            ins[0], ins[1], Common_NL_SE[case["se"]], out)
     elif op in ("low_leveling", "high_leveling", "leveling"):
         getattr(geo, op)(ins[0], ins[1], Common_NL_SE[case["se"]], out)
+    elif op == "compare":
+        from poutre2_gb300 import pixel
+        from tests.kats import COMP_VALUES, OUT_PTYPES, compare_operands
+        out = torch.empty(ins[0].shape, dtype=getattr(torch, OUT_PTYPES[case["out_ptype"]]), device="cuda")
+        pixel.CompareImage(ins[0], COMP_VALUES[case["cmp"]], *compare_operands(case, ins), out)
     elif op in ("label_binary", "label_flat_zones", "label_minima", "label_maxima"):
         from poutre2_gb300 import label
         out = torch.empty(ins[0].shape, dtype=torch.int64, device=ins[0].device)
@@ -662,3 +667,179 @@ def test_labelling_rejects_like_the_reference():
     v = dev(np.ones((4, 4, 4), np.uint8))
     with pytest.raises(PoutreError):
         label.label_binary(v, Common_NL_SE.SESquare3D, torch.empty(4, 4, 4, dtype=torch.int64, device="cuda"))
+
+
+# ----------------------------------------------------------------------------- pixel processing
+def _full(rng, dt, shape):
+    dt = np.dtype(dt)
+    if dt.kind in "iu":
+        info = np.iinfo(dt)
+        a = rng.integers(info.min, info.max, shape, dtype=dt, endpoint=True)
+        a.reshape(-1)[:4] = [info.min, info.max, info.min, info.max][: a.size]
+        return a
+    return (rng.standard_normal(shape) * 1e3).astype(dt)
+
+
+def _misaligned(a):
+    """A device copy of ``a`` that starts one pixel into its allocation (not 16-byte aligned)."""
+    buf = torch.empty(a.size + 1, dtype=getattr(torch, a.dtype.name), device="cuda")
+    v = buf[1:].view(a.shape)
+    v.copy_(torch.from_numpy(a))
+    return v
+
+
+PIXEL_SHAPES = [(1,), (17,), (5, 7), (64, 129), (3, 5, 33), (1023, 1031)]
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("kind", ["invert", "sup", "inf", "sat_add", "sat_sub"])
+def test_pixel_arith(dt, kind):
+    from poutre2_gb300 import pixel
+    fn = {"invert": pixel.ArithInvertImage, "sup": pixel.ArithSupImage, "inf": pixel.ArithInfImage,
+          "sat_add": pixel.ArithSaturatedAddImage, "sat_sub": pixel.ArithSaturatedSubImage}[kind]
+    ora = {"invert": lambda a, b: oracle.invert_image(a), "sup": oracle.sup_image, "inf": oracle.inf_image,
+           "sat_add": oracle.sat_add_image, "sat_sub": oracle.sat_sub_image}[kind]
+    rng = np.random.default_rng(hash((str(dt), kind, "gpu")) % 2**32)
+    for shape in PIXEL_SHAPES:
+        a, b = _full(rng, dt, shape), _full(rng, dt, shape)
+        if b.size >= 4:
+            b.reshape(-1)[:4] = b.reshape(-1)[[1, 0, 0, 1]]  # (min, max), (max, min), (min, min), (max, max)
+        exp = ora(a, b)
+        for mis in (False, True):
+            da, db = (_misaligned(a), _misaligned(b)) if mis else (dev(a), dev(b))
+            out = torch.empty_like(da)
+            (fn(da, out) if kind == "invert" else fn(da, db, out))
+            np.testing.assert_array_equal(host(out), exp, err_msg=f"{kind} {shape} misaligned={mis}")
+        da = dev(a)  # in place: the output is the first input
+        (fn(da, da) if kind == "invert" else fn(da, dev(b), da))
+        np.testing.assert_array_equal(host(da), exp, err_msg=f"{kind} {shape} in place")
+
+
+@pytest.mark.parametrize("dt_in", TYPES)
+@pytest.mark.parametrize("dt_out", TYPES)
+def test_compare_all_overloads(dt_in, dt_out):
+    from poutre2_gb300 import pixel
+    from tests.kats import COMP_VALUES
+    rng = np.random.default_rng(hash((str(dt_in), str(dt_out), "gpu")) % 2**32)
+    forms = ["sss", "ssi", "sis", "sii", "iss", "isi", "iis", "iii"]
+    ops = list(COMP_VALUES)
+    for j, form in enumerate(forms):
+        shape = [(1,), (33,), (7, 9), (130, 67), (4, 3, 21)][j % 5]
+        a = rng.integers(0, 4, shape).astype(dt_in)
+        opnds, dev_opnds = [], []
+        for kind, dt in zip(form, (dt_in, dt_out, dt_out)):
+            if kind == "i":
+                v = rng.integers(0, 4, shape).astype(dt)
+                opnds.append(v)
+                dev_opnds.append(dev(v))
+            else:
+                v = int(rng.integers(0, 4))
+                opnds.append(v)
+                dev_opnds.append(v)
+        for op in (ops[j % 6], ops[(j + 3) % 6]):
+            out = torch.empty(shape, dtype=getattr(torch, np.dtype(dt_out).name), device="cuda")
+            pixel.CompareImage(dev(a), COMP_VALUES[op], *dev_opnds, out)
+            np.testing.assert_array_equal(host(out), oracle.compare(a, op, *opnds, dt_out), err_msg=f"{op} {form}")
+
+
+def test_compare_misaligned_and_in_place():
+    from poutre2_gb300 import pixel
+    rng = np.random.default_rng(44)
+    a = rng.integers(0, 255, (301, 257)).astype(np.uint8)
+    t = rng.integers(0, 255, (301, 257)).astype(np.uint8)
+    exp = oracle.compare(a, "sup", 100, t, 0, np.uint8)
+    out = torch.empty(a.shape, dtype=torch.uint8, device="cuda")
+    pixel.CompareImage(_misaligned(a), pixel.CompOpType.CompOpSup, 100, _misaligned(t), 0, out)
+    np.testing.assert_array_equal(host(out), exp)
+    da = dev(a)
+    pixel.CompareImage(da, pixel.CompOpType.CompOpSup, 100, dev(t), 0, da)
+    np.testing.assert_array_equal(host(da), exp)
+
+
+@pytest.mark.parametrize("dt_in", TYPES)
+@pytest.mark.parametrize("dt_out", TYPES)
+def test_convert(dt_in, dt_out):
+    from poutre2_gb300 import pixel
+    rng = np.random.default_rng(hash((str(dt_in), str(dt_out), "gpu")) % 2**32)
+    unsigned = np.dtype(dt_in).kind == "u" or np.dtype(dt_out).kind == "u"
+    small = np.uint8 in (dt_in, dt_out)
+    lo, hi = (0 if unsigned else -1000), (255 if small else 1000)
+    for shape in [(1,), (19,), (33, 65), (2, 3, 17)]:
+        a = rng.uniform(lo, hi, shape).astype(dt_in)
+        for mis in (False, True):
+            out = torch.empty(shape, dtype=getattr(torch, np.dtype(dt_out).name), device="cuda")
+            pixel.ConvertInto(_misaligned(a) if mis else dev(a), out)
+            np.testing.assert_array_equal(host(out), oracle.convert(a, dt_out), err_msg=f"{shape} {mis}")
+    if np.dtype(dt_in).kind in "iu" and np.dtype(dt_out).kind in "iu":  # modular narrowing
+        w = _full(rng, dt_in, (33, 17))
+        out = torch.empty(w.shape, dtype=getattr(torch, np.dtype(dt_out).name), device="cuda")
+        pixel.ConvertInto(dev(w), out)
+        np.testing.assert_array_equal(host(out), oracle.convert(w, dt_out))
+
+
+def test_copy_into_and_rejections():
+    from poutre2_gb300 import pixel
+    from poutre2_gb300._lib import PoutreError
+    a = dev(np.arange(60, dtype=np.int32).reshape(6, 10))
+    o = torch.empty_like(a)
+    pixel.CopyInto(a, o)
+    assert torch.equal(a, o)
+    with pytest.raises(PoutreError):
+        pixel.CopyInto(a, torch.empty(6, 10, dtype=torch.int64, device="cuda"))  # type differs
+    with pytest.raises(PoutreError):
+        pixel.ConvertInto(a, a.view(torch.float32))  # ConvertInto images must be different
+    buf = torch.zeros(70, dtype=torch.int32, device="cuda")
+    with pytest.raises(PoutreError):  # a partial overlap of output and input
+        pixel.ArithSupImage(buf[:60].view(6, 10), a, buf[5:65].view(6, 10))
+    with pytest.raises(PoutreError):  # the comparand must have the input's type
+        pixel.CompareImage(a, pixel.CompOpType.CompOpSup, a.to(torch.int64), 1, 0, o)
+    with pytest.raises(PoutreError):  # a scalar that the pixel type cannot hold
+        pixel.CompareImage(a, pixel.CompOpType.CompOpSup, 0.5, 1, 0, o)
+
+
+def test_pypoutre_names():
+    # poutre2's Python names (python/*/*.cpp) on device images, end to end
+    from poutre2_gb300 import pypoutre as pp
+    rng = np.random.default_rng(45)
+    f = rng.integers(0, 200, (37, 53)).astype(np.uint8)
+    img = pp.from_numpy(f)
+    assert img.ptype() == pp.PType.GrayUINT8 and img.shape() == [37, 53] and img.rank() == 2
+    out = pp.clone_geometry(img)
+    pp.dilate(img, pp.static_nl_se.square2d, 2, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.erode_dilate_static(f, "SESquare2D", 2, True))
+    pp.erodeX(img, 3, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.line(f, 3, "x", False))
+    pp.h_maxima(img, 20, pp.static_nl_se.square2d, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.h_maxima(f, 20, "SESquare2D"))
+    pp.h_minima(img, 20, pp.static_nl_se.cross2d, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.h_minima(f, 20, "SECross2D"))
+    marker = pp.from_numpy(oracle.sat_sub_const(f, 30))
+    pp.reconstruction(pp.RecType.dilate, marker, img, pp.static_nl_se.square2d, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.reconstruct(oracle.sat_sub_const(f, 30), f, "SESquare2D", True))
+    pp.compare(img, pp.Comp.Sup, marker, 255, 0, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.compare(f, "sup", oracle.sat_sub_const(f, 30), 255, 0, np.uint8))
+    pp.arith_saturated_sub_image(img, marker, out)
+    np.testing.assert_array_equal(out.numpy(), oracle.sat_sub_image(f, oracle.sat_sub_const(f, 30)))
+    c = pp.convert(img, pp.CType.Scalar, pp.PType.GrayINT64)
+    assert c.ptype() == pp.PType.GrayINT64 and np.array_equal(c.numpy(), f.astype(np.int64))
+    lab = pp.factory_image([37, 53], pp.CType.Scalar, pp.PType.GrayINT64)
+    assert pp.label_flat_zones(img, pp.static_nl_se.square2d, lab) == oracle.label(f, "SESquare2D", True)[1]
+    pp.label_maxima(img, pp.static_nl_se.square2d, lab)
+    np.testing.assert_array_equal(lab.numpy(), oracle.label_extrema(f, "SESquare2D", True)[0])
+    assert pp.to_string(pp.from_string("Scalar GINT32 2 1 3 1 -2 3")) == "Scalar GINT32 2 1 3 1 -2 3"
+    # an object that exports a CUDA buffer through DLPack is taken without a copy
+
+    class Exporter:
+        def __init__(self, t):
+            self.t = t
+
+        def __dlpack__(self, **kw):
+            return self.t.__dlpack__(**kw)
+
+        def __dlpack_device__(self):
+            return self.t.__dlpack_device__()
+
+    t = torch.from_numpy(f).cuda()
+    o = torch.empty_like(t)
+    pp.arith_invert_image(Exporter(t), Exporter(o))
+    np.testing.assert_array_equal(host(o), oracle.invert_image(f))

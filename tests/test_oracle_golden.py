@@ -1,11 +1,11 @@
 """The CPU oracle reproduces every known-answer test of the reference's own test-suite
-(test/low_level_morpho/*.cpp, test/geodesy/*.cpp, test/label/label_binary.cpp, label_flat_zones.cpp, label_extrema.cpp),
+(test/low_level_morpho/*.cpp, test/geodesy/*.cpp, test/label/*.cpp, test/pixel_processing/compare.cpp),
 before it is trusted as the checker."""
 import numpy as np
 import pytest
 
 import oracle
-from tests.kats import case_id, load_cases, to_array
+from tests.kats import OUT_PTYPES, case_id, compare_operands, load_cases, to_array
 
 CASES = load_cases()
 
@@ -30,6 +30,8 @@ def run_oracle(c):
         return oracle.label(ins[0], c["se"], op == "label_flat_zones")[0]
     if op in ("label_minima", "label_maxima"):
         return oracle.label_extrema(ins[0], c["se"], op == "label_maxima")[0]
+    if op == "compare":
+        return oracle.compare(ins[0], c["cmp"], *compare_operands(c, ins), OUT_PTYPES[c["out_ptype"]])
     raise AssertionError(op)
 
 
@@ -43,8 +45,8 @@ def test_oracle_matches_reference_kat(case):
 
 def test_kat_count():
     # 20 static + 20 runtime-neighbour-list + 6 line + 4 reconstruction + 6 extrema + 4 leveling
-    # + 4 binary labelling + 2 flat-zone labelling
-    assert len(CASES) == 68
+    # + 4 binary labelling + 2 flat-zone labelling + 2 labelled extrema + 48 whole-image compares
+    assert len(CASES) == 116
 
 
 def test_oracle_dilate_y_rejects_non_square():

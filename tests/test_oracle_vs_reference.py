@@ -188,3 +188,62 @@ def test_label_extrema(dt, se, rank, maxima):
         exp = ref.label_extrema(a, se, maxima)
         assert n == int(exp.max())
         np.testing.assert_array_equal(got, exp)
+
+
+# ----------------------------------------------------------------------------- pixel processing
+def _full_range(rng, dt, shape):
+    """Values over the whole range of the type, its extremes included."""
+    dt = np.dtype(dt)
+    if dt.kind in "iu":
+        info = np.iinfo(dt)
+        a = rng.integers(info.min, info.max, shape, dtype=dt, endpoint=True)
+        flat = a.reshape(-1)
+        flat[: 4] = [info.min, info.max, info.min, info.max][: flat.size]
+        return a
+    return (rng.standard_normal(shape) * 1e3).astype(dt)
+
+
+# pixel counts that are multiples of 32, so that every pixel takes the reference's vector body
+PIXEL_SHAPES = [(8, 16), (3, 4, 32), (32, 45)]
+
+
+@pytest.mark.parametrize("dt", REF_TYPES)
+@pytest.mark.parametrize("kind", ["invert", "sup", "inf", "sat_add", "sat_sub"])
+def test_pixel_arith(dt, kind):
+    rng = np.random.default_rng(hash((str(dt), kind)) % 2**32)
+    fn = {"invert": lambda a, b: oracle.invert_image(a), "sup": oracle.sup_image, "inf": oracle.inf_image,
+          "sat_add": oracle.sat_add_image, "sat_sub": oracle.sat_sub_image}[kind]
+    for shape in PIXEL_SHAPES:
+        a, b = _full_range(rng, dt, shape), _full_range(rng, dt, shape)
+        b.reshape(-1)[:4] = b.reshape(-1)[[1, 0, 0, 1]]  # (min, max), (max, min), (min, min), (max, max)
+        np.testing.assert_array_equal(fn(a, b), ref.arith(kind, a, b), err_msg=f"{kind} {shape}")
+
+
+@pytest.mark.parametrize("dt_in", REF_TYPES)
+@pytest.mark.parametrize("dt_out", [np.uint8, np.int64, np.float32])
+@pytest.mark.parametrize("form", ["sss", "ssi", "sis", "sii", "iss", "isi", "iis", "iii"])
+def test_compare_all_overloads(dt_in, dt_out, form):
+    rng = np.random.default_rng(hash((str(dt_in), str(dt_out), form)) % 2**32)
+    shape = (9, 13)
+    a = rng.integers(0, 5, shape).astype(dt_in)
+    opnds = []
+    for kind, dt in zip(form, (dt_in, dt_out, dt_out)):
+        opnds.append(rng.integers(0, 5, shape).astype(dt) if kind == "i" else int(rng.integers(0, 5)))
+    for op in ("equal", "diff", "sup", "sup_equal", "inf", "inf_equal"):
+        got = oracle.compare(a, op, *opnds, dt_out)
+        exp = ref.compare(a, op, *opnds, dt_out)
+        np.testing.assert_array_equal(got, exp, err_msg=f"{op} {form}")
+
+
+@pytest.mark.parametrize("dt_in", REF_TYPES)
+@pytest.mark.parametrize("dt_out", REF_TYPES)
+def test_convert(dt_in, dt_out):
+    # values every output type holds (static_cast of an out-of-range float is undefined)
+    rng = np.random.default_rng(hash((str(dt_in), str(dt_out))) % 2**32)
+    lo = 0 if np.dtype(dt_out) == np.uint8 or np.dtype(dt_in) == np.uint8 else -1000
+    hi = 255 if np.dtype(dt_out) == np.uint8 or np.dtype(dt_in) == np.uint8 else 1000
+    a = rng.uniform(lo, hi, (7, 11)).astype(dt_in)
+    np.testing.assert_array_equal(oracle.convert(a, dt_out), ref.convert(a, dt_out))
+    if np.dtype(dt_in).kind == "i" and np.dtype(dt_out).kind in "iu" and np.dtype(dt_out).itemsize < np.dtype(dt_in).itemsize:
+        w = _full_range(rng, dt_in, (6, 8))  # modular narrowing
+        np.testing.assert_array_equal(oracle.convert(w, dt_out), ref.convert(w, dt_out))
