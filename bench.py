@@ -217,7 +217,8 @@ def _time_ms(fn, flush, reps=5, warm=2):
 
 def extra_measurements(dev, flush, only=None):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
-    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048), or
+    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048,
+    pixel4096), or
     all."""
     import numpy as np
     import torch
@@ -385,7 +386,49 @@ def extra_measurements(dev, flush, only=None):
                 pass
             rec(f"{name}_2048_u8", ms, img.numel(), img.numel() * 9, **kw)
 
-    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048):
+    def pixel4096():
+        # the pixel-processing kernels (HBM streams): 4096^2 u16 sup / saturated difference, the
+        # h-maxima binary compare form (image comparand, scalar true / false) on u8, and a u8 -> f32
+        # conversion; poutre2's own call on the host beside each
+        from poutre2_gb300 import pixel
+        rng = np.random.default_rng(9)
+        n = 4096 * 4096
+        a16 = rng.integers(0, 65536, (4096, 4096), dtype=np.uint16)
+        b16 = rng.integers(0, 65536, (4096, 4096), dtype=np.uint16)
+        a8 = (a16 >> 8).astype(np.uint8)
+        b8 = (b16 >> 8).astype(np.uint8)
+        x16, y16, o16 = (torch.from_numpy(a16).to(dev), torch.from_numpy(b16).to(dev),
+                         torch.empty((4096, 4096), dtype=torch.uint16, device=dev))
+        x8, y8, o8 = (torch.from_numpy(a8).to(dev), torch.from_numpy(b8).to(dev), torch.empty_like(o16, dtype=torch.uint8))
+        of = torch.empty((4096, 4096), dtype=torch.float32, device=dev)
+        work = (("sup_image_4096_u16", lambda: pixel.ArithSupImage(x16, y16, o16), 6 * n, "sup", (a16, b16)),
+                ("sat_sub_image_4096_u16", lambda: pixel.ArithSaturatedSubImage(x16, y16, o16), 6 * n, "sat_sub",
+                 (a16, b16)),
+                ("compare_sup_image_4096_u8", lambda: pixel.CompareImage(x8, pixel.CompOpType.CompOpSup, y8, 255, 0, o8),
+                 3 * n, "compare", (a8, b8)),
+                ("convert_u8_f32_4096", lambda: pixel.ConvertInto(x8, of), 5 * n, "convert", (a8,)))
+        for name, fn, nbytes, kind, host_in in work:
+            ms = _time_ms(fn, flush, 20, 5)
+            kw = {}
+            try:
+                from oracle import ref
+                if ref.available():
+                    h = [v.astype(np.int32) if v.dtype == np.uint16 else v for v in host_in]  # poutre2 has no u16
+                    t0 = time.perf_counter()
+                    if kind == "compare":
+                        ref.compare(h[0], "sup", h[1], 255, 0, np.uint8)
+                    elif kind == "convert":
+                        ref.convert(h[0], np.float32)
+                    else:
+                        ref.arith(kind, h[0], h[1])
+                    kw.update(cpu_ms=(time.perf_counter() - t0) * 1e3, cpu_kind="reference (u16 as int32)"
+                              if host_in[0].dtype == np.uint16 else "reference")
+                    kw["speedup_vs_cpu"] = kw["cpu_ms"] / ms
+            except Exception:
+                pass
+            rec(name, ms, n, nbytes, **kw)
+
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096):
         if only is None or fn.__name__ in only:
             guard(fn)
     return res
