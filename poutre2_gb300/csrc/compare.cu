@@ -48,7 +48,9 @@ template <int OP, typename TI, typename TO, bool VEC>
 __device__ __forceinline__ void compare_body(const TI *in, int op, const Operand<TI> &comp, const Operand<TO> &vt,
                                              const Operand<TO> &vf, TO *out, int64_t n) {
   constexpr int N = VEC ? chunk_pixels<TI, TO>() : 1;
-  constexpr int U = VEC ? unroll_of<TI, TO, 2>() : 1;
+  // sized for an image comparand and scalar true / false values (the binary-output form); image
+  // true / false values add to the chunks held
+  constexpr int U = VEC ? unroll_for<2 * N * (int)sizeof(TI), 2 * N * (int)(sizeof(TI) + sizeof(TO))>() : 1;
   const int64_t chunks = n / N, stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (int64_t c0 = t0; c0 < chunks; c0 += U * stride) {

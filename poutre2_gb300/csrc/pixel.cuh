@@ -40,13 +40,14 @@ template <typename A, typename B> __host__ __device__ constexpr int chunk_pixels
   return 16 / (int)(sizeof(A) < sizeof(B) ? sizeof(A) : sizeof(B));
 }
 
-// Chunks in flight per thread and loop turn: all loads of a turn are issued before its first store
-// (one 16-byte load per thread alone leaves HBM latency-bound); the U chunks of a turn are one grid
-// stride apart, so each warp access stays contiguous.  Fewer when the wider type makes chunks big.
-template <typename A, typename B, int MAXU> __host__ __device__ constexpr int unroll_of() {
-  constexpr int r = 8 * (int)(sizeof(A) < sizeof(B) ? sizeof(A) : sizeof(B)) /
-                    (int)(sizeof(A) < sizeof(B) ? sizeof(B) : sizeof(A));
-  return r < 1 ? 1 : (r > MAXU ? MAXU : r);
+// Chunks in flight per thread and loop turn: all loads of a turn are issued before its first store,
+// aiming at LOAD bytes of loads per chunk x U = 128 bytes in flight per thread (one 16-byte load per
+// thread leaves HBM latency-bound), with at most HOLD bytes x U = 256 bytes of chunks held in
+// registers; the U chunks of a turn are one grid stride apart, so each warp access stays contiguous.
+template <int LOAD, int HOLD> __host__ __device__ constexpr int unroll_for() {
+  constexpr int a = 128 / LOAD, b = 256 / HOLD;
+  constexpr int u = a < b ? a : b;
+  return u < 1 ? 1 : (u > 8 ? 8 : u);
 }
 
 inline unsigned grid_for_chunks(int64_t chunks) {
