@@ -197,15 +197,20 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- GPU arm
 def _time_ms(fn, flush, reps=5, warm=2):
-    """Median CUDA-event time of fn() on the current stream, L2 flushed before each rep."""
+    """Median CUDA-event time of fn() on the current stream, L2 flushed before each rep.  A GPU-side
+    wait of about 100 us is queued after the flush, so that fn's launches are already enqueued when
+    the stream reaches the first event: the bracket times the device work, not the host's launch
+    path (which for a 10-20 us kernel is of the same order)."""
     import torch
     for _ in range(warm):
         fn()
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
+    spin = 200_000  # SM cycles: ~100 us at 2 GHz
     out = []
     for _ in range(reps):
         flush_l2(flush)
+        torch.cuda._sleep(spin)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(st)
         fn()

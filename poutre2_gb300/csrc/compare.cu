@@ -28,6 +28,30 @@ template <int OP, typename T> __device__ __forceinline__ bool comp_op(int op, T 
   else return a <= b;  // PG_COMP_INF_EQUAL
 }
 
+// per-byte / per-halfword compare masks (0xff / 0xffff where true) for 8- / 16-bit unsigned pixels
+template <int OP, typename T> __device__ __forceinline__ uint32_t comp_mask(int op, uint32_t a, uint32_t b) {
+  const int o = OP == 0 ? op : OP;
+  if constexpr (sizeof(T) == 1) {
+    switch (o) {
+      case PG_COMP_EQUAL: return __vcmpeq4(a, b);
+      case PG_COMP_DIFF: return __vcmpne4(a, b);
+      case PG_COMP_SUP: return __vcmpgtu4(a, b);
+      case PG_COMP_SUP_EQUAL: return __vcmpgeu4(a, b);
+      case PG_COMP_INF: return __vcmpltu4(a, b);
+      default: return __vcmpleu4(a, b);
+    }
+  } else {
+    switch (o) {
+      case PG_COMP_EQUAL: return __vcmpeq2(a, b);
+      case PG_COMP_DIFF: return __vcmpne2(a, b);
+      case PG_COMP_SUP: return __vcmpgtu2(a, b);
+      case PG_COMP_SUP_EQUAL: return __vcmpgeu2(a, b);
+      case PG_COMP_INF: return __vcmpltu2(a, b);
+      default: return __vcmpleu2(a, b);
+    }
+  }
+}
+
 // an operand of CompareImage on the device: an image, or (p == nullptr) a scalar of its type
 template <typename T> struct Operand {
   const T *p;
@@ -71,8 +95,16 @@ __device__ __forceinline__ void compare_body(const TI *in, int op, const Operand
       const int64_t c = c0 + u * stride;
       if (c < chunks) {
         Chunk<TO, N> r;
+        if constexpr (VEC && kPacked<TI> && std::is_same_v<TI, TO>) {
 #pragma unroll
-        for (int k = 0; k < N; ++k) r.v[k] = comp_op<OP>(op, x[u].v[k], y[u].v[k]) ? t[u].v[k] : f[u].v[k];
+          for (int k = 0; k < 4; ++k) {
+            const uint32_t m = comp_mask<OP, TI>(op, words(x[u])[k], words(y[u])[k]);
+            words(r)[k] = (words(t[u])[k] & m) | (words(f[u])[k] & ~m);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < N; ++k) r.v[k] = comp_op<OP>(op, x[u].v[k], y[u].v[k]) ? t[u].v[k] : f[u].v[k];
+        }
         chunk_store(out + c * N, r);
       }
     }

@@ -34,6 +34,23 @@ template <int OP, typename T> __device__ __forceinline__ T arith(T a, T b) {
   else return negate(a);
 }
 
+// the same operation on the four bytes / two halfwords of a word
+template <int OP, typename T> __device__ __forceinline__ uint32_t arith_word(uint32_t a, uint32_t b) {
+  if constexpr (sizeof(T) == 1) {
+    if constexpr (OP == PX_INF) return __vminu4(a, b);
+    else if constexpr (OP == PX_SUP) return __vmaxu4(a, b);
+    else if constexpr (OP == PX_SADD) return __vaddus4(a, b);
+    else if constexpr (OP == PX_SSUB) return __vsubus4(a, b);
+    else return __vneg4(a);
+  } else {
+    if constexpr (OP == PX_INF) return __vminu2(a, b);
+    else if constexpr (OP == PX_SUP) return __vmaxu2(a, b);
+    else if constexpr (OP == PX_SADD) return __vaddus2(a, b);
+    else if constexpr (OP == PX_SSUB) return __vsubus2(a, b);
+    else return __vneg2(a);
+  }
+}
+
 template <typename T, int OP, bool VEC>
 __global__ void __launch_bounds__(kPThreads) k_arith(const T *a, const T *b, T *o, int64_t n) {
   constexpr int N = VEC ? 16 / (int)sizeof(T) : 1;
@@ -55,8 +72,13 @@ __global__ void __launch_bounds__(kPThreads) k_arith(const T *a, const T *b, T *
       const int64_t c = c0 + u * stride;
       if (c < chunks) {
         Chunk<T, N> r;
+        if constexpr (VEC && kPacked<T>) {
 #pragma unroll
-        for (int k = 0; k < N; ++k) r.v[k] = arith<OP>(x[u].v[k], OP != PX_NEG ? y[u].v[k] : T(0));
+          for (int k = 0; k < 4; ++k) words(r)[k] = arith_word<OP, T>(words(x[u])[k], words(y[u])[k]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < N; ++k) r.v[k] = arith<OP>(x[u].v[k], OP != PX_NEG ? y[u].v[k] : T(0));
+        }
         chunk_store(o + c * N, r);
       }
     }

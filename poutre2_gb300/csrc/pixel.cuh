@@ -50,6 +50,17 @@ template <int LOAD, int HOLD> __host__ __device__ constexpr int unroll_for() {
   return u < 1 ? 1 : (u > 8 ? 8 : u);
 }
 
+// 8- and 16-bit pixels of one type are processed four / two per 32-bit word with the CUDA SIMD
+// intrinsics (__vminu4, __vcmpgtu2, ...), which give the per-pixel results bit for bit.
+template <typename T> inline constexpr bool kPacked = std::is_same_v<T, uint8_t> || std::is_same_v<T, uint16_t>;
+
+template <typename T, int N> __device__ __forceinline__ uint32_t *words(Chunk<T, N> &c) {
+  return reinterpret_cast<uint32_t *>(c.v);
+}
+template <typename T, int N> __device__ __forceinline__ const uint32_t *words(const Chunk<T, N> &c) {
+  return reinterpret_cast<const uint32_t *>(c.v);
+}
+
 inline unsigned grid_for_chunks(int64_t chunks) {
   int64_t b = ceil_div(chunks > 0 ? chunks : 1, kPThreads);
   const int64_t cap = (int64_t)num_sms() * (2048 / kPThreads);  // one full wave of resident CTAs
