@@ -74,7 +74,7 @@ __device__ __forceinline__ void compare_body(const TI *in, int op, const Operand
   constexpr int N = VEC ? chunk_pixels<TI, TO>() : 1;
   // sized for an image comparand and scalar true / false values (the binary-output form); image
   // true / false values add to the chunks held
-  constexpr int U = VEC ? unroll_for<2 * N * (int)sizeof(TI), 2 * N * (int)(sizeof(TI) + sizeof(TO))>() : 1;
+  constexpr int U = VEC ? unroll_for<2 * N * (int)sizeof(TI), 2 * N * (int)(sizeof(TI) + sizeof(TO)), 128, 128>() : 1;
   const int64_t chunks = n / N, stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (int64_t c0 = t0; c0 < chunks; c0 += U * stride) {

@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kPThreads) k_arith(const T *a, const T *b, T *
 template <typename TI, typename TO, bool VEC>
 __global__ void __launch_bounds__(kPThreads) k_convert(const TI *in, TO *out, int64_t n) {
   constexpr int N = VEC ? chunk_pixels<TI, TO>() : 1;
-  constexpr int U = VEC ? unroll_for<N * (int)sizeof(TI), N * (int)sizeof(TI)>() : 1;
+  constexpr int U = VEC ? unroll_for<N * (int)sizeof(TI), N * (int)sizeof(TI), 64>() : 1;
   const int64_t chunks = n / N, stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (int64_t c0 = t0; c0 < chunks; c0 += U * stride) {

@@ -44,8 +44,9 @@ template <typename A, typename B> __host__ __device__ constexpr int chunk_pixels
 // aiming at LOAD bytes of loads per chunk x U = 128 bytes in flight per thread (one 16-byte load per
 // thread leaves HBM latency-bound), with at most HOLD bytes x U = 256 bytes of chunks held in
 // registers; the U chunks of a turn are one grid stride apart, so each warp access stays contiguous.
-template <int LOAD, int HOLD> __host__ __device__ constexpr int unroll_for() {
-  constexpr int a = 128 / LOAD, b = 256 / HOLD;
+template <int LOAD, int HOLD, int LOAD_BUDGET = 128, int HOLD_BUDGET = 256>
+__host__ __device__ constexpr int unroll_for() {
+  constexpr int a = LOAD_BUDGET / LOAD, b = HOLD_BUDGET / HOLD;
   constexpr int u = a < b ? a : b;
   return u < 1 ? 1 : (u > 8 ? 8 : u);
 }
