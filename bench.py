@@ -223,7 +223,7 @@ def _time_ms(fn, flush, reps=5, warm=2):
 def extra_measurements(dev, flush, only=None):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
     `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048,
-    pixel4096), or
+    pixel4096, octagon4096), or
     all."""
     import numpy as np
     import torch
@@ -433,7 +433,29 @@ def extra_measurements(dev, flush, only=None):
                 pass
             rec(name, ms, n, nbytes, **kw)
 
-    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096):
+    def octagon4096():
+        # the octagon compound SE (size crosses and squares fused in one tile kernel), 4096^2 u8 / u16
+        from poutre2_gb300.se import Compound_NL_SE
+        rng = np.random.default_rng(10)
+        for dt, tdt in ((np.uint8, torch.uint8), (np.uint16, torch.uint16)):
+            a = rng.integers(0, np.iinfo(dt).max, (4096, 4096), dtype=dt, endpoint=True)
+            x = torch.from_numpy(a).to(dev)
+            o = torch.empty_like(x)
+            for size in (5, 10):
+                ms = _time_ms(lambda: llm.Dilate(x, Compound_NL_SE.Octagon, size, o), flush, 10, 3)
+                kw = {}
+                try:
+                    from oracle import ref
+                    if ref.available() and dt == np.uint8:
+                        t0 = time.perf_counter()
+                        ref.erode_dilate_compound(a, "Octagon", size, True)
+                        kw.update(cpu_ms=(time.perf_counter() - t0) * 1e3, cpu_kind="reference")
+                        kw["speedup_vs_cpu"] = kw["cpu_ms"] / ms
+                except Exception:
+                    pass
+                rec(f"octagon{size}_dilate_4096_{np.dtype(dt).name}", ms, a.size, 2 * a.nbytes, **kw)
+
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096, octagon4096):
         if only is None or fn.__name__ in only:
             guard(fn)
     return res

@@ -117,6 +117,29 @@ def erode(img, se: str = "SESquare2D", iterations: int = 1):
     return erode_dilate_static(img, se, iterations, False)
 
 
+def compound_passes(cse: str, size: int):
+    """The passes of t_DilateOctagon / t_DilateRhombicuboctahedron
+    (low_level_morpho/details/ero_dil_compound_static_se_t.hpp:34-95): `size` passes, the last
+    round(size / (1 + sqrt 2)) (halves rounded up) by the square, the others by the cross."""
+    cross, square = ("SECross2D", "SESquare2D") if cse == "Octagon" else ("SECross3D", "SESquare3D")
+    if size <= 0:
+        return []
+    if size == 1:
+        return ["SECross2D"]  # the reference's size-1 case uses the 2D cross for both
+    nb = size / (1 + np.sqrt(2.0))
+    nsq = int(np.floor(nb) if nb - np.floor(nb) < 0.5 else np.floor(nb) + 1)
+    return [cross] * (size - nsq) + [square] * nsq
+
+
+def erode_dilate_compound(img, cse: str, size: int, dilate: bool = True) -> np.ndarray:
+    """poutre::Erode/Dilate(i_img, Compound_NL_SE, size, o_img) (src/low_level_morpho/ero_dil_compound_static.cpp):
+    the static passes of compound_passes() in order."""
+    a = _c(img).copy()
+    for se in compound_passes(cse, size):
+        a = erode_dilate_static(a, se, 1, dilate)
+    return a
+
+
 def erode_dilate_nl(img, offsets, dilate: bool = True) -> np.ndarray:
     """poutre::Erode/Dilate(i_img, IStructuringElement, o_img) with a neighbour list
     (src/low_level_morpho/ero_dil.cpp:59,152; ero_dil_runtime_nl_se_t.hpp:54-96).

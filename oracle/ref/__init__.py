@@ -72,6 +72,14 @@ def erode_dilate_static(img, se, iterations=1, dilate=True):
     return out
 
 
+def erode_dilate_compound(img, cse, size, dilate=True):
+    """poutre::Erode/Dilate(i_img, Compound_NL_SE, size, o_img) on the compiled reference."""
+    a = np.ascontiguousarray(img); out = np.empty_like(a)
+    _chk(lib().ref_erode_dilate_compound(PTYPE[a.dtype], a.ndim, _shape(a), _p(a), _p(out),
+                                         {"Octagon": 1, "Rhombicuboctahedron": 2}[cse], int(size), int(dilate)))
+    return out
+
+
 def erode_dilate_nl(img, offsets, dilate=True):
     a = np.ascontiguousarray(img); out = np.empty_like(a)
     o = np.ascontiguousarray(np.array(offsets, dtype=np.int32).reshape(-1, a.ndim))

@@ -138,6 +138,20 @@ int ref_erode_dilate_static(int pt, int rank, const int64_t *shape, const void *
   });
 }
 
+// poutre::Erode / poutre::Dilate (const IInterface&, Compound_NL_SE, int size, IInterface&)
+// include/poutre/low_level_morpho/ero_dil.hpp:38-41
+int ref_erode_dilate_compound(int pt, int rank, const int64_t *shape, const void *in, void *out, int cse,
+                              int size, int dilate) {
+  return guarded([&] {
+    auto a = make(pt, rank, shape, in);
+    auto b = make(pt, rank, shape, nullptr);
+    auto c = static_cast<poutre::se::Compound_NL_SE>(cse);
+    if (dilate) poutre::Dilate(*a, c, size, *b);
+    else poutre::Erode(*a, c, size, *b);
+    take(*b, pt, rank, shape, out);
+  });
+}
+
 // poutre::Erode / Dilate (const IInterface&, const IStructuringElement&, IInterface&)
 // include/poutre/low_level_morpho/ero_dil.hpp:44-47; offs = n x rank ints, reference order.
 int ref_erode_dilate_nl(int pt, int rank, const int64_t *shape, const void *in, void *out,

@@ -169,6 +169,24 @@ def test_compound(cse, rank):
         np.testing.assert_array_equal(host(out), exp, err_msg=f"size={size}")
 
 
+@pytest.mark.parametrize("dt", TYPES)
+def test_octagon_fused(dt):
+    # the one-kernel octagon (sizes 2..16) and the pass sequence beyond, against the oracle's passes,
+    # on images smaller than, equal to and not a multiple of the 64 x 64 tile
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Compound_NL_SE
+    rng = np.random.default_rng(hash((str(dt), "octagon")) % 2**32)
+    for shape in [(1, 1), (1, 90), (77, 1), (64, 64), (130, 67), (203, 300)]:
+        a = rand(rng, shape, dt)
+        x = dev(a)
+        for size in (2, 3, 5, 8, 13, 16, 17):
+            for dil in (True, False):
+                out = torch.empty_like(x)
+                (llm.Dilate if dil else llm.Erode)(x, Compound_NL_SE.Octagon, size, out)
+                np.testing.assert_array_equal(host(out), oracle.erode_dilate_compound(a, "Octagon", size, dil),
+                                              err_msg=f"{shape} size={size} dilate={dil}")
+
+
 # ----------------------------------------------------------------------------- neighbour lists, lines
 @pytest.mark.parametrize("dt", TYPES)
 def test_neighbor_list(dt):
