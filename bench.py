@@ -434,7 +434,7 @@ def extra_measurements(dev, flush, only=None):
             rec(name, ms, n, nbytes, **kw)
 
     def octagon4096():
-        # the octagon compound SE (size crosses and squares fused in one tile kernel), 4096^2 u8 / u16
+        # the octagon compound SE (its cross passes, then one box for the trailing squares), 4096^2 u8 / u16
         from poutre2_gb300.se import Compound_NL_SE
         rng = np.random.default_rng(10)
         for dt, tdt in ((np.uint8, torch.uint8), (np.uint16, torch.uint16)):

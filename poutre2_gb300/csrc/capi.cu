@@ -212,8 +212,6 @@ static pg_status compound(const pg_image &in, int compound_se, int size, const p
   const double nb = (double)size / (1.0 + std::sqrt(2.0));
   const double fl = std::floor(nb);
   const int nb_square = (int)((nb - fl) < 0.5 ? fl : fl + 1);
-  if (compound_se == PG_COMPOUND_OCTAGON && octagon_fused_ok(in, size))
-    return launch_octagon_fused(in, out, size - nb_square, nb_square, dilate, s);
   std::vector<int> passes;
   passes.push_back(cross);
   for (int i = 1; i < size - nb_square; ++i) passes.push_back(cross);

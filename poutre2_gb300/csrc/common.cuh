@@ -238,11 +238,6 @@ pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, 
 pg_status launch_sat_const(const pg_image &in, double v, bool add, const pg_image &out, cudaStream_t s);
 pg_status launch_sat_sub_image(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
 
-// octagon.cu: the octagon compound SE (n_cross cross passes, then n_square square passes) in one kernel
-bool octagon_fused_ok(const pg_image &in, int size);
-pg_status launch_octagon_fused(const pg_image &in, const pg_image &out, int n_cross, int n_square, bool dilate,
-                               cudaStream_t s);
-
 // pixel.cu: ArithInf/Sup/SaturatedAdd/SaturatedSub/Invert image, CompareImage, ConvertInto
 enum PixelOp { PX_INF = 0, PX_SUP = 1, PX_SADD = 2, PX_SSUB = 3, PX_NEG = 4 };
 pg_status launch_pixel_arith(int op, const pg_image &a, const pg_image *b, const pg_image &out, cudaStream_t s);

@@ -170,9 +170,9 @@ def test_compound(cse, rank):
 
 
 @pytest.mark.parametrize("dt", TYPES)
-def test_octagon_fused(dt):
-    # the one-kernel octagon (sizes 2..16) and the pass sequence beyond, against the oracle's passes,
-    # on images smaller than, equal to and not a multiple of the 64 x 64 tile
+def test_octagon_sizes(dt):
+    # the octagon's cross passes and fused trailing box against the oracle's passes (pinned against
+    # poutre2's compound Dilate / Erode), on small, thin and ragged images
     from poutre2_gb300 import llm
     from poutre2_gb300.se import Compound_NL_SE
     rng = np.random.default_rng(hash((str(dt), "octagon")) % 2**32)
