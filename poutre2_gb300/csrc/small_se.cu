@@ -116,37 +116,6 @@ __device__ __forceinline__ void load_row(const T *__restrict__ row, bool valid, 
   h = P::template op<SUP>(P::template op<SUP>(c, c.shl(left)), c.shr(right));
 }
 
-// one row's loads: the centre pack and its two edge pixels (neutral outside the image), fetched one
-// loop turn before they are combined so that two rows of loads are in flight per thread
-template <typename T, typename P> struct RowLoads {
-  P c;
-  T l, r;
-};
-
-template <typename T, bool SUP, typename P>
-__device__ __forceinline__ RowLoads<T, P> fetch_row(const T *__restrict__ row, bool valid, int64_t x0, int64_t W,
-                                                    bool need_h) {
-  const T NEU = Op<T, SUP>::neutral();
-  RowLoads<T, P> w;
-  if (!valid) {
-    w.c = P::fill(NEU);
-    w.l = NEU;
-    w.r = NEU;
-    return w;
-  }
-  w.c = P::load(row + x0);
-  w.l = (need_h && x0 > 0) ? ldg(row + x0 - 1) : NEU;
-  w.r = (need_h && x0 + P::N < W) ? ldg(row + x0 + P::N) : NEU;
-  return w;
-}
-
-template <typename T, bool SUP, typename P>
-__device__ __forceinline__ void finish_row(const RowLoads<T, P> &w, bool need_h, P &c, P &h) {
-  c = w.c;
-  if (!need_h) { h = c; return; }
-  h = P::template op<SUP>(P::template op<SUP>(c, c.shl(w.l)), c.shr(w.r));
-}
-
 // 2D: SESquare2D / SECross2D / SESegmentX2D / SESegmentY2D (and SESegmentX1D as H == 1).
 template <typename T, bool SUP, int SHAPE, typename P>
 __global__ void __launch_bounds__(256) k_small2d(const T *__restrict__ in, T *__restrict__ out, int64_t H, int64_t W,
@@ -160,12 +129,8 @@ __global__ void __launch_bounds__(256) k_small2d(const T *__restrict__ in, T *__
   P cp, hp, cc, hc, cn, hn;
   load_row<T, SUP>(in + (y0 - 1) * W, y0 >= 1, x0, W, NEED_H, cp, hp);
   load_row<T, SUP>(in + y0 * W, true, x0, W, NEED_H, cc, hc);
-  // rows y0 - 1 .. y1 are read; row y + 2 is fetched while row y is computed
-  RowLoads<T, P> next = fetch_row<T, SUP, P>(in + (y0 + 1) * W, y0 + 1 < H, x0, W, NEED_H);
   for (int64_t y = y0; y < y1; ++y) {
-    const RowLoads<T, P> ahead = fetch_row<T, SUP, P>(in + (y + 2) * W, y + 2 <= y1 && y + 2 < H, x0, W, NEED_H);
-    finish_row<T, SUP>(next, NEED_H, cn, hn);
-    next = ahead;
+    load_row<T, SUP>(in + (y + 1) * W, y + 1 < H, x0, W, NEED_H, cn, hn);
     P r;
     if constexpr (SHAPE == SH_SQUARE) r = P::template op<SUP>(P::template op<SUP>(hp, hc), hn);
     else if constexpr (SHAPE == SH_CROSS) r = P::template op<SUP>(P::template op<SUP>(cp, hc), cn);
