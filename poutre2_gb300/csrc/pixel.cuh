@@ -64,12 +64,16 @@ template <typename T, int N> __device__ __forceinline__ const uint32_t *words(co
 
 inline unsigned grid_for_chunks(int64_t chunks) {
   int64_t b = ceil_div(chunks > 0 ? chunks : 1, kPThreads);
-  const int64_t cap = (int64_t)num_sms() * (2048 / kPThreads);  // one full wave of resident CTAs
+  // 8 CTAs of 256 threads per SM: one wave at the SM's 2048-thread limit (variants whose registers
+  // allow fewer resident CTAs run it in several)
+  const int64_t cap = (int64_t)num_sms() * (2048 / kPThreads);
   return (unsigned)(b < cap ? b : cap);
 }
 
 inline bool aligned16(const void *p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; }
 
+// PG_DISPATCH_PTYPE under a second name, for the output type inside a dispatch on the input type (a
+// macro is not expanded again inside its own expansion)
 #define PG_DISPATCH_PTYPE2(pt, T, ...)                                        \
   switch (pt) {                                                               \
     case PG_PTYPE_U8: { using T = uint8_t; __VA_ARGS__; } break;              \
