@@ -177,3 +177,20 @@ def test_pypoutre_mirror_names_and_enums():
     assert int(pp.Comp.Sup) == 4 and int(pp.PType.GrayUINT8) == 4 and int(pp.RecType.dilate) == 1
     with pytest.raises(Exception):
         pp.Image(__import__("torch").zeros(3, 3))  # a host tensor is no device image
+
+
+def test_pixel_and_pypoutre_refuse_host_images():
+    # no CPU path: host tensors are refused before the library is called
+    import torch
+    from poutre2_gb300 import pixel
+    from poutre2_gb300 import pypoutre as pp
+    from poutre2_gb300._lib import PoutreError
+    h = torch.zeros(4, 4, dtype=torch.uint8)
+    with pytest.raises(PoutreError):
+        pixel.ArithSupImage(h, h, torch.zeros_like(h))
+    with pytest.raises(PoutreError):
+        pixel.CompareImage(h, pixel.CompOpType.CompOpSup, 1, 255, 0, torch.zeros_like(h))
+    with pytest.raises(PoutreError):
+        pp.dilate(h, pp.static_nl_se.square2d, 1, torch.zeros_like(h))
+    with pytest.raises(PoutreError):
+        pp.label_maxima(h, pp.static_nl_se.square2d, torch.zeros(4, 4, dtype=torch.int64))
