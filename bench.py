@@ -223,7 +223,7 @@ def _time_ms(fn, flush, reps=5, warm=2):
 def extra_measurements(dev, flush, only=None):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
     `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048,
-    pixel4096, octagon4096), or
+    pixel4096, octagon4096, geodesy3d), or
     all."""
     import numpy as np
     import torch
@@ -455,7 +455,30 @@ def extra_measurements(dev, flush, only=None):
                     pass
                 rec(f"octagon{size}_dilate_4096_{np.dtype(dt).name}", ms, a.size, 2 * a.nbytes, **kw)
 
-    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096, octagon4096):
+    def geodesy3d():
+        # binary h-maxima (h = 10) of a 128^3 u8 volume (white noise, Gaussian sigma 2, rescaled), both
+        # 3D SEs: the iterated geodesic step of the volume route, poutre2 on one core beside it
+        from scipy.ndimage import gaussian_filter
+        rng = np.random.default_rng(12)
+        v = gaussian_filter(rng.standard_normal((128, 128, 128)), 2.0, mode="reflect", truncate=4.0)
+        f = np.rint((v - v.min()) / (v.max() - v.min()) * 255).astype(np.uint8)
+        x = torch.from_numpy(f).to(dev)
+        o = torch.empty_like(x)
+        for se in ("SECross3D", "SESquare3D"):
+            ms = _time_ms(lambda se=se: geo.h_maxima_binary(x, 10, Common_NL_SE[se], o, check=False), flush, 5, 2)
+            kw = {"note": "includes the host reads of the change flag (every 8 steps)"}
+            try:
+                from oracle import ref
+                if ref.available():
+                    t0 = time.perf_counter()
+                    ref.extrema("h_maxima", f, 10, se)
+                    kw.update(cpu_ms=(time.perf_counter() - t0) * 1e3, cpu_kind="reference (h_maxima, compare not timed)")
+                    kw["speedup_vs_cpu"] = kw["cpu_ms"] / ms
+            except Exception:
+                pass
+            rec(f"h_maxima_binary_{se}_128cube_u8", ms, f.size, 2 * f.size, **kw)
+
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096, octagon4096, geodesy3d):
         if only is None or fn.__name__ in only:
             guard(fn)
     return res

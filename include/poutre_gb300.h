@@ -163,8 +163,8 @@ PG_API pg_status pg_label_flat_zones(const pg_image *in, int32_t common_se, cons
 
 /* poutre::label::label_minima / label_maxima(const IInterface&, se::Common_NL_SE, IInterface&),
  * include/poutre/label/label_extrema.hpp (src/label/label_extrema.cpp): the regional minima /
- * maxima, labelled: label_binary of h_concave(f, 1) / h_convex(f, 1).  Integer images; SEs of the
- * reconstruction (SESegmentX1D, SESquare2D, SECross2D); output and nb_labels as label_binary. */
+ * maxima, labelled: label_binary of h_concave(f, 1) / h_convex(f, 1).  Integer images; SESegmentX1D,
+ * SESquare2D, SECross2D, SECross3D; output and nb_labels as label_binary. */
 PG_API pg_status pg_label_minima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
                                  pg_stream_t stream);
 PG_API pg_status pg_label_maxima(const pg_image *in, int32_t common_se, const pg_image *out, int64_t *nb_labels,
@@ -174,7 +174,10 @@ PG_API pg_status pg_label_maxima(const pg_image *in, int32_t common_se, const pg
 
 /* poutre::geo::Reconstruction(reconstruction_type, const IInterface& marker, const IInterface& mask,
  * se::Common_NL_SE, IInterface&), include/poutre/geodesy/mreconstruct.hpp:37-41.
- * 1D (SESegmentX1D) and 2D (SESquare2D, SECross2D) SEs; pixel types u8, u16, i32, i64, f32, f64. */
+ * 1D (SESegmentX1D), 2D (SESquare2D, SECross2D) and 3D (SECross3D, SESquare3D) SEs; pixel types u8,
+ * u16, i32, i64, f32, f64.  Volumes iterate the geodesic step (extremum over the SE clamped to the
+ * mask) to its fixpoint, one launch per step, the host reading a change flag every 8 steps; the
+ * h-extrema, dynamic pseudo filters, leveling and binary h-maxima of volumes take the same route. */
 PG_API pg_status pg_reconstruction(int32_t type, const pg_image *marker, const pg_image *mask, int32_t common_se,
                             const pg_image *out, pg_stream_t stream);
 
@@ -195,7 +198,8 @@ PG_API pg_status pg_dynamic_pseudo_closing(const pg_image *in, double h, int32_t
 PG_API pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
 
 /* Ragged batch of the binary h-maxima: n independent 2D images of any sizes in ONE persistent
- * launch (tile table over all images).  ins[i]/outs[i] are device images (outs u8). */
+ * launch (tile table over all images).  ins[i]/outs[i] are device images (outs u8); volumes are
+ * taken one after the other by the 3D route of pg_reconstruction. */
 PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t common_se,
                                    pg_stream_t stream);
 
@@ -205,7 +209,7 @@ PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *o
  * With autotune != 0 the plan times tile side (32: register tiles, a warp per tile; 64: shared-
  * memory tiles, a 64-thread CTA per tile) x sweep sets per tile visit (4, 16, unbounded) on this
  * batch and keeps the fastest; the choice is cached per (pixel type, connectivity, batch size
- * class).  Without autotune the configuration is 32 / unbounded.  Inputs/outputs must stay valid
+ * class).  Without autotune the configuration is 32 / unbounded.  Images of rank 1 or 2.  Inputs/outputs must stay valid
  * while the plan is used.  Plan creation synchronises the device.
  * pg_batch_plan_set_config pins the configuration: tile 32 or 64 (64 only for pixels of at most
  * 4 bytes), sweeps >= 1 (a tile that reaches the cap yields and is revisited next round). */
@@ -229,8 +233,9 @@ PG_API pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_
 
 /* ---------------------------------------------------------------- pixel_processing subset */
 
-/* poutre::ArithSaturatedSubConstant / ArithSaturatedAddConstant (src/pixel_processing/arith.cpp:471),
- * integer pixel types. */
+/* poutre::ArithSaturatedSubConstant / ArithSaturatedAddConstant (src/pixel_processing/arith.cpp:471):
+ * integers clamp to the pixel type's range, floating point is the plain IEEE result (as for the
+ * saturated image arithmetic below); `v` must be representable in the pixel type. */
 PG_API pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
 PG_API pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
 

@@ -302,8 +302,8 @@ static pg_status recon_se(int se, int rank, bool &conn8) {
   if (rank == 1 && se == PG_SE_SEGMENT_X_1D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_SQUARE_2D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_CROSS_2D) { conn8 = false; return PG_OK; }
-  if (rank == 3 && (se == PG_SE_CROSS_3D || se == PG_SE_SQUARE_3D))
-    return fail(PG_ERR_UNSUPPORTED_SE, "3D reconstruction is not available on the GPU path");
+  if (rank == 3 && se == PG_SE_SQUARE_3D) { conn8 = true; return PG_OK; }
+  if (rank == 3 && se == PG_SE_CROSS_3D) { conn8 = false; return PG_OK; }
   return fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
 }
 
@@ -330,6 +330,7 @@ static pg_status label_extrema(const pg_image *in, int32_t se, const pg_image *o
   if (in->ptype == PG_PTYPE_F32 || in->ptype == PG_PTYPE_F64)
     return fail(PG_ERR_UNSUPPORTED_PTYPE, "label_binary of a float image is not on the GPU path");
   if (se_rank(se) == 0 || se_rank(se) != in->rank) return fail(PG_ERR_UNSUPPORTED_SE, "t_label_binaryDispatch unsupported nl_static");
+  if (se == PG_SE_SQUARE_3D) return fail(PG_ERR_UNSUPPORTED_SE, "SESquare3D labelling is not on the GPU path");
   bool conn8;
   PG_TRY(recon_se(se, in->rank, conn8));  // the h-extrema reconstruction's own SE rule
   const size_t bytes = (size_t)dims_of(*in).count() * elem_size(in->ptype);
@@ -589,6 +590,7 @@ pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *out
     if (dims_of(ins[i]).count() == 0) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch_plan: empty image");
   }
   PG_TRY(check_scalar(ins[0].ptype, h, "h_maxima_binary_batch_plan"));
+  if (ins[0].rank == 3) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch_plan: images of rank 1 or 2");
   bool conn8 = true;
   PG_TRY(recon_se(se, ins[0].rank, conn8));
   return create_batch_plan(ins, outs, n, h, conn8, autotune != 0, STREAM(s), plan);

@@ -266,6 +266,10 @@ struct ReconRequest {
 pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
                                 const ReconRequest &rq, cudaStream_t s);
 
+// recon3d.cu: the same request for one volume (rank 3; conn8 = SESquare3D, else SECross3D)
+pg_status launch_reconstruction3d(const pg_image *marker, const pg_image &mask, const pg_image &out,
+                                  const ReconRequest &rq, cudaStream_t s);
+
 pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, double h, bool conn8, bool autotune,
                             cudaStream_t s, pg_batch_plan **out_plan);
 pg_status run_batch_plan(pg_batch_plan *p, cudaStream_t s);

@@ -1281,6 +1281,11 @@ static pg_status run_dispatch(std::vector<RImg> &imgs, const ReconRequest &rq, c
 pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
                                 const ReconRequest &rq, cudaStream_t s) {
   if (n_images < 1) return PG_OK;
+  if (masks[0].rank == 3) {  // volumes: the iterated geodesic step of recon3d.cu, one volume at a time
+    for (int i = 0; i < n_images; ++i)
+      PG_TRY(launch_reconstruction3d(markers ? &markers[i] : nullptr, masks[i], outs[i], rq, s));
+    return PG_OK;
+  }
   std::vector<RImg> imgs((size_t)n_images);
   for (int i = 0; i < n_images; ++i) {
     const Dims d = dims_of(masks[i]);

@@ -861,3 +861,88 @@ def test_pypoutre_names():
     o = torch.empty_like(t)
     pp.arith_invert_image(Exporter(t), Exporter(o))
     np.testing.assert_array_equal(host(o), oracle.invert_image(f))
+
+
+# ----------------------------------------------------------------------------- 3D geodesy
+def _volume(seed, shape, dt):
+    rng = np.random.default_rng(seed)
+    v = rng.integers(0, 60, shape)
+    return v.astype(dt)
+
+
+@pytest.mark.parametrize("dt", TYPES)
+@pytest.mark.parametrize("se", ["SECross3D", "SESquare3D"])
+def test_reconstruction_3d(dt, se):
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    for k, shape in enumerate([(1, 1, 1), (1, 1, 40), (5, 6, 7), (20, 33, 40)]):
+        mask = _volume(k, shape, dt)
+        for dil in (True, False):
+            mk = (mask // 2).astype(dt) if dil else (mask + 25).astype(dt)
+            out = torch.empty_like(dev(mask))
+            geo.Reconstruction(geo.reconstruction_type.dilate if dil else geo.reconstruction_type.erode,
+                               dev(mk), dev(mask), Common_NL_SE[se], out)
+            np.testing.assert_array_equal(host(out), oracle.reconstruct(mk, mask, se, dil), err_msg=f"{shape} {dil}")
+
+
+def test_reconstruction_3d_long_path():
+    # a corridor that winds through the slices: the fixpoint needs hundreds of steps
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    D, H, W = 8, 24, 30
+    mask = np.zeros((D, H, W), np.uint8)
+    for z in range(D):
+        for r in range(0, H, 3):
+            mask[z, r, :] = 150
+            c = W - 1 if (r // 3) % 2 == 0 else 0
+            mask[z, r:r + 3, c] = 150
+        mask[z, H - 1 if z % 2 == 0 else 0, :] = 150
+    marker = np.zeros_like(mask)
+    marker[0, 0, 0] = 150
+    for se in ("SECross3D", "SESquare3D"):
+        out = torch.empty_like(dev(mask))
+        geo.Reconstruction(geo.reconstruction_type.dilate, dev(marker), dev(mask), Common_NL_SE[se], out)
+        np.testing.assert_array_equal(host(out), oracle.reconstruct(marker, mask, se, True), err_msg=se)
+
+
+@pytest.mark.parametrize("kind", ["h_minima", "h_maxima", "h_convex", "h_concave", "dynamic_pseudo_opening",
+                                  "dynamic_pseudo_closing"])
+def test_extrema_3d(kind):
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    for dt in (np.uint8, np.int32):
+        f = _volume(31, (9, 17, 23), dt)
+        for se in ("SECross3D", "SESquare3D"):
+            out = torch.empty_like(dev(f))
+            getattr(geo, kind)(dev(f), 7, Common_NL_SE[se], out)
+            np.testing.assert_array_equal(host(out), getattr(oracle, kind)(f, 7, se), err_msg=f"{se} {dt}")
+
+
+@pytest.mark.parametrize("kind", ["low_leveling", "high_leveling", "leveling"])
+def test_leveling_3d(kind):
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    for dt in (np.uint8, np.float32):
+        ref = _volume(41, (7, 15, 19), dt)
+        marker = _volume(42, (7, 15, 19), dt)
+        for se in ("SECross3D", "SESquare3D"):
+            out = torch.empty_like(dev(ref))
+            getattr(geo, kind)(dev(ref), dev(marker), Common_NL_SE[se], out)
+            np.testing.assert_array_equal(host(out), getattr(oracle, kind)(ref, marker, se), err_msg=f"{se} {dt}")
+
+
+def test_h_maxima_binary_and_label_extrema_3d():
+    from poutre2_gb300 import geo, label
+    from poutre2_gb300.se import Common_NL_SE
+    f = _volume(51, (10, 21, 26), np.uint8)
+    x = dev(f)
+    for se in ("SECross3D", "SESquare3D"):
+        b = torch.empty_like(x)
+        geo.h_maxima_binary(x, 5, Common_NL_SE[se], b)
+        np.testing.assert_array_equal(host(b), oracle.h_maxima_binary(f, 5, se), err_msg=se)
+    for maxima in (False, True):
+        out = torch.empty(f.shape, dtype=torch.int64, device="cuda")
+        n = (label.label_maxima if maxima else label.label_minima)(x, Common_NL_SE.SECross3D, out)
+        exp, m = oracle.label_extrema(f, "SECross3D", maxima)
+        assert n == m
+        np.testing.assert_array_equal(host(out), exp)

@@ -271,3 +271,22 @@ def test_compound_rhombicuboctahedron(dilate):
         if size >= 2:
             continue  # the reference's slice-wise SESquare3D / SECross3D passes are defective (recorded)
         np.testing.assert_array_equal(got, exp, err_msg=f"size={size}")
+
+
+@pytest.mark.parametrize("dt", REF_TYPES)
+@pytest.mark.parametrize("se", ["SECross3D", "SESquare3D"])
+def test_geodesy_3d(dt, se):
+    # reconstruction, h-extrema and leveling of volumes (the oracle is also the GPU's checker here)
+    if np.dtype(dt).kind == "f":
+        pytest.skip("the reference reconstructs u8, i32 and i64 only")
+    rng = np.random.default_rng(hash((str(dt), se, "3d")) % 2**32)
+    for shape in [(1, 1, 1), (4, 5, 6), (9, 8, 10)]:
+        mask = rng.integers(0, 60, shape).astype(dt)
+        for dil in (True, False):
+            mk = (mask // 2).astype(dt) if dil else (mask + 25).astype(dt)
+            np.testing.assert_array_equal(oracle.reconstruct(mk, mask, se, dil), ref.reconstruct(mk, mask, se, dil))
+        for kind in ("h_maxima", "h_minima"):
+            np.testing.assert_array_equal(getattr(oracle, kind)(mask, 7, se), ref.extrema(kind, mask, 7, se))
+        marker = rng.integers(0, 60, shape).astype(dt)
+        for kind in ("low_leveling", "high_leveling", "leveling"):
+            np.testing.assert_array_equal(getattr(oracle, kind)(mask, marker, se), ref.leveling(kind, mask, marker, se))
