@@ -456,15 +456,15 @@ def extra_measurements(dev, flush, only=None):
                 rec(f"octagon{size}_dilate_4096_{np.dtype(dt).name}", ms, a.size, 2 * a.nbytes, **kw)
 
     def geodesy3d():
-        # binary h-maxima (h = 10) of a 128^3 u8 volume (white noise, Gaussian sigma 2, rescaled), both
-        # 3D SEs: the iterated geodesic step of the volume route, poutre2 on one core beside it
+        # binary h-maxima (h = 10) of a 128^3 u8 volume (white noise, Gaussian sigma 2, rescaled),
+        # SECross3D: the iterated geodesic step of the volume route, poutre2 on one core beside it
         from scipy.ndimage import gaussian_filter
         rng = np.random.default_rng(12)
         v = gaussian_filter(rng.standard_normal((128, 128, 128)), 2.0, mode="reflect", truncate=4.0)
         f = np.rint((v - v.min()) / (v.max() - v.min()) * 255).astype(np.uint8)
         x = torch.from_numpy(f).to(dev)
         o = torch.empty_like(x)
-        for se in ("SECross3D", "SESquare3D"):
+        for se in ("SECross3D",):
             ms = _time_ms(lambda se=se: geo.h_maxima_binary(x, 10, Common_NL_SE[se], o, check=False), flush, 5, 2)
             kw = {"note": "includes the host reads of the change flag (every 8 steps)"}
             try:

@@ -174,10 +174,12 @@ PG_API pg_status pg_label_maxima(const pg_image *in, int32_t common_se, const pg
 
 /* poutre::geo::Reconstruction(reconstruction_type, const IInterface& marker, const IInterface& mask,
  * se::Common_NL_SE, IInterface&), include/poutre/geodesy/mreconstruct.hpp:37-41.
- * 1D (SESegmentX1D), 2D (SESquare2D, SECross2D) and 3D (SECross3D, SESquare3D) SEs; pixel types u8,
+ * 1D (SESegmentX1D), 2D (SESquare2D, SECross2D) and 3D (SECross3D) SEs; pixel types u8,
  * u16, i32, i64, f32, f64.  Volumes iterate the geodesic step (extremum over the SE clamped to the
  * mask) to its fixpoint, one launch per step, the host reading a change flag every 8 steps; the
- * h-extrema, dynamic pseudo filters, leveling and binary h-maxima of volumes take the same route. */
+ * h-extrema, dynamic pseudo filters, leveling and binary h-maxima of volumes take the same route.
+ * SESquare3D is refused (PG_ERR_UNSUPPORTED_SE): poutre2's schedule stops short of the fixpoint for
+ * it on thin volumes, so no GPU result could match it. */
 PG_API pg_status pg_reconstruction(int32_t type, const pg_image *marker, const pg_image *mask, int32_t common_se,
                             const pg_image *out, pg_stream_t stream);
 

@@ -302,8 +302,11 @@ static pg_status recon_se(int se, int rank, bool &conn8) {
   if (rank == 1 && se == PG_SE_SEGMENT_X_1D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_SQUARE_2D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_CROSS_2D) { conn8 = false; return PG_OK; }
-  if (rank == 3 && se == PG_SE_SQUARE_3D) { conn8 = true; return PG_OK; }
   if (rank == 3 && se == PG_SE_CROSS_3D) { conn8 = false; return PG_OK; }
+  // poutre2's raster / anti-raster schedule stops short of the fixpoint for SESquare3D (it differs
+  // from the iterated geodesic dilation on thin volumes), so no GPU result could match it
+  if (rank == 3 && se == PG_SE_SQUARE_3D)
+    return fail(PG_ERR_UNSUPPORTED_SE, "SESquare3D reconstruction is not on the GPU path");
   return fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
 }
 
@@ -330,7 +333,6 @@ static pg_status label_extrema(const pg_image *in, int32_t se, const pg_image *o
   if (in->ptype == PG_PTYPE_F32 || in->ptype == PG_PTYPE_F64)
     return fail(PG_ERR_UNSUPPORTED_PTYPE, "label_binary of a float image is not on the GPU path");
   if (se_rank(se) == 0 || se_rank(se) != in->rank) return fail(PG_ERR_UNSUPPORTED_SE, "t_label_binaryDispatch unsupported nl_static");
-  if (se == PG_SE_SQUARE_3D) return fail(PG_ERR_UNSUPPORTED_SE, "SESquare3D labelling is not on the GPU path");
   bool conn8;
   PG_TRY(recon_se(se, in->rank, conn8));  // the h-extrema reconstruction's own SE rule
   const size_t bytes = (size_t)dims_of(*in).count() * elem_size(in->ptype);

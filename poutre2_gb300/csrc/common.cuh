@@ -266,7 +266,7 @@ struct ReconRequest {
 pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
                                 const ReconRequest &rq, cudaStream_t s);
 
-// recon3d.cu: the same request for one volume (rank 3; conn8 = SESquare3D, else SECross3D)
+// recon3d.cu: the same request for one volume (rank 3, SECross3D)
 pg_status launch_reconstruction3d(const pg_image *marker, const pg_image &mask, const pg_image &out,
                                   const ReconRequest &rq, cudaStream_t s);
 

@@ -1,11 +1,12 @@
-// recon3d.cu -- geodesic reconstruction of volumes (rank 3, SECross3D / SESquare3D) and, through the
-// same request, the 3D h-extrema, dynamic pseudo filters, leveling and binary h-maxima.
+// recon3d.cu -- geodesic reconstruction of volumes (rank 3, SECross3D) and, through the same request,
+// the 3D h-extrema, dynamic pseudo filters, leveling and binary h-maxima.
 //
 // Reference: t_ReconstructionViewDispatcher (geodesy/details/mreconstruct_t.hpp:84-195, 3D SEs at
 // :469-474) and t_low/high_levelingHelper (geodesy/details/leveling_t.hpp:45-202, 3D at :260-340).
 // The reconstruction is the least fixpoint of the geodesic dilation g -> min(dilate(g), mask) (the
-// dual for erosion) from the clamped marker; poutre2's raster / anti-raster / FIFO schedule reaches it
-// and so does iterating the geodesic dilation until nothing changes, which is what runs here:
+// dual for erosion) from the clamped marker; for SECross3D poutre2's raster / anti-raster / FIFO
+// schedule reaches it and so does iterating the geodesic dilation until nothing changes, which is
+// what runs here (for SESquare3D poutre2 stops short of it, and that SE is refused):
 //   prep     -- the initial value (marker clamped to the mask, or the mask shifted by h) and, for
 //               leveling, the effective mask max(marker, ref) / min(marker, ref);
 //   step     -- one voxel per thread: the extremum over the SE's voxels inside the volume, clamped to
@@ -43,7 +44,7 @@ __global__ void k_r3_prep(const T *__restrict__ ref, const T *__restrict__ marke
   }
 }
 
-template <typename T, bool SUP, bool SQUARE>
+template <typename T, bool SUP>
 __global__ void __launch_bounds__(256) k_r3_step(const T *__restrict__ cur, const T *__restrict__ mask,
                                                  T *__restrict__ next, int D, int H, int W, int *__restrict__ changed) {
   const int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -53,28 +54,13 @@ __global__ void __launch_bounds__(256) k_r3_step(const T *__restrict__ cur, cons
   if (x < W && y < H) {
     const int64_t c = ((int64_t)z * H + y) * W + x;
     const T v0 = cur[c];
-    T v = v0;
-    if constexpr (SQUARE) {
-#pragma unroll
-      for (int dz = -1; dz <= 1; ++dz) {
-        if (z + dz < 0 || z + dz >= D) continue;
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy) {
-          if (y + dy < 0 || y + dy >= H) continue;
-          const T *row = cur + ((int64_t)(z + dz) * H + (y + dy)) * W;
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx)
-            if (x + dx >= 0 && x + dx < W) v = Op<T, SUP>::apply(v, row[x + dx]);
-        }
-      }
-    } else {
-      if (x > 0) v = Op<T, SUP>::apply(v, cur[c - 1]);
-      if (x + 1 < W) v = Op<T, SUP>::apply(v, cur[c + 1]);
-      if (y > 0) v = Op<T, SUP>::apply(v, cur[c - W]);
-      if (y + 1 < H) v = Op<T, SUP>::apply(v, cur[c + W]);
-      if (z > 0) v = Op<T, SUP>::apply(v, cur[c - (int64_t)H * W]);
-      if (z + 1 < D) v = Op<T, SUP>::apply(v, cur[c + (int64_t)H * W]);
-    }
+    T v = v0;  // the SECross3D voxels inside the volume
+    if (x > 0) v = Op<T, SUP>::apply(v, cur[c - 1]);
+    if (x + 1 < W) v = Op<T, SUP>::apply(v, cur[c + 1]);
+    if (y > 0) v = Op<T, SUP>::apply(v, cur[c - W]);
+    if (y + 1 < H) v = Op<T, SUP>::apply(v, cur[c + W]);
+    if (z > 0) v = Op<T, SUP>::apply(v, cur[c - (int64_t)H * W]);
+    if (z + 1 < D) v = Op<T, SUP>::apply(v, cur[c + (int64_t)H * W]);
     v = Op<T, !SUP>::apply(v, mask[c]);
     next[c] = v;
     diff = !(v == v0);
@@ -99,7 +85,7 @@ unsigned flat_grid(int64_t n) {
   return (unsigned)(b < cap ? b : cap);
 }
 
-template <typename T, bool SUP, bool SQUARE>
+template <typename T, bool SUP>
 pg_status recon3d_t(const pg_image *marker, const pg_image &mask, const pg_image &out, const ReconRequest &rq,
                     cudaStream_t s) {
   const Dims d = dims_of(mask);
@@ -127,7 +113,7 @@ pg_status recon3d_t(const pg_image *marker, const pg_image &mask, const pg_image
   for (;;) {
     PG_CUDA_TRY(cudaMemsetAsync(d_flag, 0, sizeof(int), s), "3D reconstruction flag reset");
     for (int k = 0; k < kStepBatch; ++k) {
-      k_r3_step<T, SUP, SQUARE><<<grid, block, 0, s>>>(a, eff, b, (int)d.nz, (int)d.ny, (int)d.nx, d_flag);
+      k_r3_step<T, SUP><<<grid, block, 0, s>>>(a, eff, b, (int)d.nz, (int)d.ny, (int)d.nx, d_flag);
       T *t = a;
       a = b;
       b = t;
@@ -150,10 +136,7 @@ pg_status launch_reconstruction3d(const pg_image *marker, const pg_image &mask, 
                                   const ReconRequest &rq, cudaStream_t s) {
   if (mask.rank != 3) return fail(PG_ERR_INVALID_ARGUMENT, "3D reconstruction of a non-3D image");
   PG_DISPATCH_PTYPE(mask.ptype, T, {
-    if (rq.dilate) return rq.conn8 ? recon3d_t<T, true, true>(marker, mask, out, rq, s)
-                                   : recon3d_t<T, true, false>(marker, mask, out, rq, s);
-    return rq.conn8 ? recon3d_t<T, false, true>(marker, mask, out, rq, s)
-                    : recon3d_t<T, false, false>(marker, mask, out, rq, s);
+    return rq.dilate ? recon3d_t<T, true>(marker, mask, out, rq, s) : recon3d_t<T, false>(marker, mask, out, rq, s);
   });
   return PG_OK;
 }

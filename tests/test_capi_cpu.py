@@ -194,3 +194,22 @@ def test_pixel_and_pypoutre_refuse_host_images():
         pp.dilate(h, pp.static_nl_se.square2d, 1, torch.zeros_like(h))
     with pytest.raises(PoutreError):
         pp.label_maxima(h, pp.static_nl_se.square2d, torch.zeros(4, 4, dtype=torch.int64))
+
+
+def test_square3d_reconstruction_is_refused_before_device_work(lib_path):
+    # poutre2's SESquare3D reconstruction stops short of the fixpoint on thin volumes: not on the GPU path
+    import ctypes
+    from poutre2_gb300 import _lib
+    L = _lib.load()
+
+    def img(shape, data):
+        d = _lib.PgImage()
+        d.data, d.ptype, d.rank = data, 4, len(shape)
+        for i, s in enumerate(shape):
+            d.shape[i] = s
+        return d
+
+    m, k, o = img((4, 4, 4), 0x10000), img((4, 4, 4), 0x20000), img((4, 4, 4), 0x30000)
+    B = ctypes.byref
+    assert L.pg_reconstruction(1, B(m), B(k), 10, B(o), None) == 3
+    assert L.pg_h_maxima(B(m), 5.0, 10, B(o), None) == 3

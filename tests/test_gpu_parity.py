@@ -871,7 +871,7 @@ def _volume(seed, shape, dt):
 
 
 @pytest.mark.parametrize("dt", TYPES)
-@pytest.mark.parametrize("se", ["SECross3D", "SESquare3D"])
+@pytest.mark.parametrize("se", ["SECross3D"])
 def test_reconstruction_3d(dt, se):
     from poutre2_gb300 import geo
     from poutre2_gb300.se import Common_NL_SE
@@ -899,10 +899,9 @@ def test_reconstruction_3d_long_path():
         mask[z, H - 1 if z % 2 == 0 else 0, :] = 150
     marker = np.zeros_like(mask)
     marker[0, 0, 0] = 150
-    for se in ("SECross3D", "SESquare3D"):
-        out = torch.empty_like(dev(mask))
-        geo.Reconstruction(geo.reconstruction_type.dilate, dev(marker), dev(mask), Common_NL_SE[se], out)
-        np.testing.assert_array_equal(host(out), oracle.reconstruct(marker, mask, se, True), err_msg=se)
+    out = torch.empty_like(dev(mask))
+    geo.Reconstruction(geo.reconstruction_type.dilate, dev(marker), dev(mask), Common_NL_SE.SECross3D, out)
+    np.testing.assert_array_equal(host(out), oracle.reconstruct(marker, mask, "SECross3D", True))
 
 
 @pytest.mark.parametrize("kind", ["h_minima", "h_maxima", "h_convex", "h_concave", "dynamic_pseudo_opening",
@@ -912,7 +911,7 @@ def test_extrema_3d(kind):
     from poutre2_gb300.se import Common_NL_SE
     for dt in (np.uint8, np.int32):
         f = _volume(31, (9, 17, 23), dt)
-        for se in ("SECross3D", "SESquare3D"):
+        for se in ("SECross3D",):
             out = torch.empty_like(dev(f))
             getattr(geo, kind)(dev(f), 7, Common_NL_SE[se], out)
             np.testing.assert_array_equal(host(out), getattr(oracle, kind)(f, 7, se), err_msg=f"{se} {dt}")
@@ -925,7 +924,7 @@ def test_leveling_3d(kind):
     for dt in (np.uint8, np.float32):
         ref = _volume(41, (7, 15, 19), dt)
         marker = _volume(42, (7, 15, 19), dt)
-        for se in ("SECross3D", "SESquare3D"):
+        for se in ("SECross3D",):
             out = torch.empty_like(dev(ref))
             getattr(geo, kind)(dev(ref), dev(marker), Common_NL_SE[se], out)
             np.testing.assert_array_equal(host(out), getattr(oracle, kind)(ref, marker, se), err_msg=f"{se} {dt}")
@@ -936,7 +935,7 @@ def test_h_maxima_binary_and_label_extrema_3d():
     from poutre2_gb300.se import Common_NL_SE
     f = _volume(51, (10, 21, 26), np.uint8)
     x = dev(f)
-    for se in ("SECross3D", "SESquare3D"):
+    for se in ("SECross3D",):
         b = torch.empty_like(x)
         geo.h_maxima_binary(x, 5, Common_NL_SE[se], b)
         np.testing.assert_array_equal(host(b), oracle.h_maxima_binary(f, 5, se), err_msg=se)
