@@ -290,3 +290,14 @@ def test_geodesy_3d(dt, se):
         marker = rng.integers(0, 60, shape).astype(dt)
         for kind in ("low_leveling", "high_leveling", "leveling"):
             np.testing.assert_array_equal(getattr(oracle, kind)(mask, marker, se), ref.leveling(kind, mask, marker, se))
+
+
+@pytest.mark.parametrize("maxima", [False, True])
+def test_label_extrema_3d(maxima):
+    rng = np.random.default_rng(61 + maxima)
+    for shape in [(1, 1, 1), (4, 5, 6), (7, 9, 8)]:
+        a = rng.integers(0, 6, shape).astype(np.uint8)
+        got, n = oracle.label_extrema(a, "SECross3D", maxima)
+        exp = ref.label_extrema(a, "SECross3D", maxima)
+        assert n == int(exp.max())
+        np.testing.assert_array_equal(got, exp, err_msg=f"{shape}")
