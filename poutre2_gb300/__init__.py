@@ -5,5 +5,10 @@ from ``csrc/``) of hand-written CUDA kernels.  The Python modules mirror poutre2
 public API on device images (torch CUDA tensors) and call that library through
 ctypes; there is no CPU fallback: every entry point raises if the library or a GPU
 is missing.
+
+Modules: ``llm`` (erosion / dilation, openings, lines), ``geo`` (reconstruction, h-extrema,
+leveling, the ragged h-maxima batch), ``label`` (connected components, labelled extrema),
+``pixel`` (arithmetic, CompareImage, conversion), ``autograd`` (flat-morphology adjoint),
+``pypoutre`` (the nanobind module's own names), ``image`` / ``se`` (images, SEs).
 """
 from .se import Common_NL_SE, Compound_NL_SE, NeighborList, predefined_offsets  # noqa: F401
