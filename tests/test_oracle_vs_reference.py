@@ -301,3 +301,13 @@ def test_label_extrema_3d(maxima):
         exp = ref.label_extrema(a, "SECross3D", maxima)
         assert n == int(exp.max())
         np.testing.assert_array_equal(got, exp, err_msg=f"{shape}")
+
+
+@pytest.mark.parametrize("kind", ["h_convex", "h_concave", "dynamic_pseudo_opening", "dynamic_pseudo_closing"])
+def test_extrema_3d(kind):
+    rng = np.random.default_rng(hash((kind, "3d")) % 2**32)
+    for dt in (np.uint8, np.int32):
+        for shape in [(1, 1, 1), (5, 6, 7), (8, 9, 10)]:
+            f = rng.integers(0, 60, shape).astype(dt)
+            np.testing.assert_array_equal(getattr(oracle, kind)(f, 7, "SECross3D"), ref.extrema(kind, f, 7, "SECross3D"),
+                                          err_msg=f"{dt} {shape}")
