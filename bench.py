@@ -131,6 +131,36 @@ def workload_image(size):
     return synthetic.smoothed_noise_u8((size, size), seed=1, sigma=4.0)
 
 
+def workload_name(size):
+    """The workload string of both arms' `config` (identical, so that the two lines compare)."""
+    return (f"binary h-maxima (sat_sub h={H_VALUE}, reconstruction by dilation 8-conn to idempotence, "
+            f"mask>rec) {size}x{size} u8 smoothed noise sigma=4 seed 1")
+
+
+def host_cpu():
+    """Model name and logical core count of the host CPU (the CPU baseline's machine)."""
+    model = platform.processor() or ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                model = v.strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith(("model name", "cpu part")):
+                        model = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"cpu_model": model or "unknown", "nproc": os.cpu_count() or 1, "arch": platform.machine()}
+
+
 # ----------------------------------------------------------------------------- CPU baseline
 def cpu_hmaxima_fn():
     """poutre2's CPU binary h-maxima (oracle/_ref) or, failing that, the C restatement:
@@ -150,21 +180,37 @@ def cpu_hmaxima_fn():
     return (lambda img, h: oracle.h_maxima_binary(img, h, "SESquare2D")), "port"
 
 
-def cpu_hmaxima(f, budget_s=12.0, min_runs=1):
-    """Time poutre2's CPU implementation (oracle/_ref) or, failing that, the C restatement on
-    `f`; returns (pixels/s, kind, runs)."""
+def cpu_threads():
+    """Host threads for the CPU leg: every core this process may run on."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
+def cpu_hmaxima(f, budget_s=12.0, min_runs=1, threads=1, max_runs=50):
+    """Time poutre2's CPU implementation (oracle/_ref) or, failing that, the C restatement on `f`.
+
+    poutre2 is single-threaded, so with threads > 1 each host thread runs the whole workload on its own
+    copy of the image at the same time (independent replicas, as the GPU arm's ranks are); one run is
+    the wall time until every thread has finished its image.  Returns (pixels/s over all threads, kind,
+    runs)."""
+    import concurrent.futures
     hm, kind = cpu_hmaxima_fn()
-    fn = lambda: hm(f, H_VALUE)  # noqa: E731
-    fn()  # warm
-    times = []
-    t_end = time.perf_counter() + budget_s
-    while len(times) < min_runs or time.perf_counter() < t_end:
-        t0 = time.perf_counter()
-        fn()
-        times.append(time.perf_counter() - t0)
-        if len(times) >= 50:
-            break
-    return f.size / statistics.median(times), kind, len(times)
+    copies = [f.copy() for _ in range(threads)]
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:  # ctypes calls release the GIL
+        def one():
+            list(ex.map(lambda c: hm(c, H_VALUE), copies))
+        one()  # warm
+        times = []
+        t_end = time.perf_counter() + budget_s
+        while len(times) < min_runs or time.perf_counter() < t_end:
+            t0 = time.perf_counter()
+            one()
+            times.append(time.perf_counter() - t0)
+            if len(times) >= max_runs:
+                break
+    return threads * f.size / statistics.median(times), kind, len(times)
 
 
 def run_reference(args):
@@ -172,22 +218,24 @@ def run_reference(args):
     if rank != 0:
         return 0
     f = workload_image(args.size)
-    steps = []
+    th = cpu_threads()
     for _ in range(args.warmup):
-        cpu_hmaxima(f, budget_s=0.0)
+        cpu_hmaxima(f, budget_s=0.0, threads=th)
+    steps = []
     for _ in range(args.steps):
-        v, kind, runs = cpu_hmaxima(f, budget_s=0.0)
-        steps.append(1.0 / v * f.size)
+        v, kind, runs = cpu_hmaxima(f, budget_s=0.0, threads=th)
+        steps.append(th * f.size / v)
     t = statistics.mean(steps)
-    value = f.size / t / 1e9
+    value = th * f.size / t / 1e9
+    v1, _, runs1 = cpu_hmaxima(f, budget_s=0.0, min_runs=3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": f"binary h-maxima (sat_sub h={H_VALUE}, reconstruction by dilation 8-conn, mask>rec) "
-                                   f"{args.size}x{args.size} u8 smoothed noise sigma=4 seed 1"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
-                             "sample": f"{args.steps} full runs of the {args.size}^2 workload, single thread "
-                                       f"(poutre2 has no threading)",
+            "config": {"workload": workload_name(args.size), "parallelism": f"replicas x{ws}"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": th, "kind": kind, **host_cpu(),
+                             "sample": f"each step: {th} host threads each run the full {args.size}^2 workload on "
+                                       f"its own copy (poutre2 is single-threaded; replicas, as on the GPU arm)",
+                             "single_thread_value": v1 / 1e9,
                              "build": f"g++ -O3 ({platform.machine()}; xsimd stand-in of fixed-width lane "
                                       f"loops, auto-vectorised by the compiler)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -541,9 +589,17 @@ def run_gpu(args):
     _lib.call("pg_check_device", None)
     value = replica_value(N, ws, t_step)
 
-    # parity of the timed output against the oracle (outside the timed region)
+    # parity of the timed output against the oracle and against poutre2 itself (outside the timed region)
     import oracle
-    parity = bool(np.array_equal(out.cpu().numpy(), oracle.h_maxima_binary(f, H_VALUE, "SESquare2D")))
+    got = out.cpu().numpy()
+    parity = bool(np.array_equal(got, oracle.h_maxima_binary(f, H_VALUE, "SESquare2D")))
+    parity_ref = None
+    try:
+        from oracle import ref
+        if ref.available():
+            parity_ref = bool(np.array_equal(got, ref.h_maxima_binary(f, H_VALUE, "SESquare2D")))
+    except Exception:
+        parity_ref = None
 
     # end to end through the public API: pinned host input -> device -> result -> pinned host
     hin = torch.from_numpy(f).pin_memory()
@@ -570,11 +626,9 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u8", "data": "synthetic",
-        "config": {"workload": f"binary h-maxima (sat_sub h={H_VALUE}, reconstruction by dilation 8-conn to "
-                               f"idempotence, mask>rec) {args.size}x{args.size} u8 smoothed noise sigma=4 seed 1",
-                   "l2": "flushed between timed steps (256 MB read, untimed)", "rounds": rounds,
-                   "parallelism": f"replicas x{ws}"},
-        "parity_vs_oracle": parity,
+        "config": {"workload": workload_name(args.size), "parallelism": f"replicas x{ws}",
+                   "l2": "flushed between timed steps (256 MB read, untimed)", "rounds": rounds},
+        "parity_vs_oracle": parity, "parity_vs_reference": parity_ref,
         "e2e": {"value": replica_value(N, ws, t_e2e), "unit": UNIT, "h2d_bytes_per_step": int(N), "d2h_bytes_per_step": int(N)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_for(f"k_reconstruct_wl@hmaxima{args.size}"),
@@ -585,10 +639,13 @@ def run_gpu(args):
     }
     if rank == 0:
         if not args.no_cpu:
-            v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget)
-            line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": 1, "kind": kind,
-                                    "sample": f"{runs} runs of the full {args.size}^2 workload on one host core "
-                                              f"(poutre2 is single-threaded)",
+            th = cpu_threads()
+            v, kind, runs = cpu_hmaxima(f, budget_s=args.cpu_budget, threads=th)
+            v1, _, runs1 = cpu_hmaxima(f, budget_s=min(args.cpu_budget, 5.0))
+            line["cpu_baseline"] = {"value": v / 1e9, "unit": UNIT, "cores": th, "kind": kind, **host_cpu(),
+                                    "sample": f"{runs} runs; each run: {th} host threads each run the full "
+                                              f"{args.size}^2 workload on its own copy (poutre2 is single-threaded)",
+                                    "single_thread_value": v1 / 1e9, "single_thread_runs": runs1,
                                     "build": f"g++ -O3 ({platform.machine()}; xsimd stand-in of fixed-width lane "
                                              f"loops, auto-vectorised by the compiler)"}
         if args.extra:

@@ -307,15 +307,18 @@ PG_API pg_status pg_flat_morph2d_backward(const float *x, const float *grad_out,
  * it exists for callers that cannot allocate -- e.g. a real-time imaging pipeline that
  * reserves all of its device memory up front and forbids cudaMalloc in steady state (an
  * allocation may synchronise the device or fail under memory pressure), or a host that gives
- * this library a fixed memory budget.  Same arguments, checks and result as
- * pg_reconstruction (1D and 2D SEs); the caller still provides marker, mask and output.
+ * this library a fixed memory budget.  Same arguments, checks (in the same order) and result
+ * as pg_reconstruction, for 1D and 2D images; a volume is refused with PG_ERR_UNSUPPORTED_SE.
+ * The caller still provides marker, mask and output.
  * Its scratch (control block + tile worklist) is a 1 MiB file-scope device array that every
  * GPU loading the library holds until exit, so the image may span at most 131040 tiles
- * (64x64 pixels; 32x32 for 8-byte pixels) -- about 536 Mpixel for 1..4-byte pixels -- and
- * larger images are rejected with PG_ERR_INVALID_ARGUMENT.  All calls share that array: calls
- * that overlap on the GPU (other streams, other threads) race and must be serialised by the
- * caller.  The first call on a device looks the array's address up; make it before any
- * stream capture.  Device-side failure is reported by pg_check_device, as for the others. */
+ * (64x64 pixels; 32x32 for 8-byte pixels) -- about 536 Mpixel for 1..4-byte pixels, 134 Mpixel
+ * for 8-byte pixels -- and larger images are rejected with PG_ERR_INVALID_ARGUMENT.  All calls
+ * share that array: calls that overlap on the GPU (other streams, other threads) race and must
+ * be serialised by the caller.  The first call on a device looks the array's address up and
+ * keeps it; make that call before any stream capture, and do not call this entry point again
+ * on a device after cudaDeviceReset.  Device-side failure is reported by pg_check_device, as
+ * for the others. */
 PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const pg_image *mask,
                                            int32_t common_se, const pg_image *out, pg_stream_t stream);
 

@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY (checker + CPU baseline).  Recipe:
 
-1. ``stage``: when the poutre2 tree is available (``POUTRE2_REFERENCE``, default
-   ``/root/reference``), copy the headers under ``include/poutre`` and the ``.cpp`` files
+1. ``stage``: when the poutre2 tree is given (the ``root`` argument, else the environment
+   variable ``POUTRE2_REFERENCE``), copy the headers under ``include/poutre`` and the ``.cpp`` files
    of the modules on the path (base, pixel_processing, structuring_element,
    low_level_morpho, geodesy) and of label into ``oracle/_ref/src``.  ``oracle/_ref`` is git-ignored,
    so no reference source enters the repository; the staged copy only lets the same
@@ -34,13 +34,18 @@ LIB = os.path.join(OUT, "libpoutre_ref.so")
 MODULES = ["base", "pixel_processing", "structuring_element", "low_level_morpho", "geodesy", "label"]
 
 
-def reference_root():
-    return os.environ.get("POUTRE2_REFERENCE", "/root/reference")
+def reference_root(root: str | None = None) -> str | None:
+    """The poutre2 source tree: `root`, else $POUTRE2_REFERENCE, else None (no default)."""
+    return root or os.environ.get("POUTRE2_REFERENCE") or None
 
 
-def stage() -> bool:
-    root = reference_root()
-    if not os.path.isdir(os.path.join(root, "include", "poutre")):
+def has_tree(root: str | None) -> bool:
+    return bool(root) and os.path.isdir(os.path.join(root, "include", "poutre"))
+
+
+def stage(root: str | None = None) -> bool:
+    root = reference_root(root)
+    if not has_tree(root):
         return os.path.isdir(STAGE)
     if os.path.isdir(STAGE):
         shutil.rmtree(STAGE)
@@ -90,14 +95,14 @@ def compile_lib(jobs: int | None = None) -> str:
     return LIB
 
 
-def build() -> str | None:
-    """Stage (when the tree is mounted) and compile; returns the library path or None."""
-    if not stage():
+def build(root: str | None = None) -> str | None:
+    """Stage (when the tree is given) and compile; returns the library path or None."""
+    if not stage(root):
         return None
     return compile_lib()
 
 
 if __name__ == "__main__":
-    p = build()
+    p = build(sys.argv[1] if len(sys.argv) > 1 else None)
     print(p or "poutre2 sources unavailable: oracle/_ref not built")
     sys.exit(0)

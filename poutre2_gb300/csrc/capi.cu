@@ -85,7 +85,7 @@ static bool overlaps(const pg_image &a, const pg_image &b) {
 }
 
 // in -> out of the same geometry and type, distinct buffers
-static pg_status check_in_out(const pg_image *in, const pg_image *out, const char *what) {
+pg_status check_in_out(const pg_image *in, const pg_image *out, const char *what) {
   PG_TRY(check_image(in, what));
   PG_TRY(check_image(out, what));
   if (!same_geometry(*in, *out)) return fail(PG_ERR_INCOMPATIBLE, std::string(what) + " images have not compatible sizes");
@@ -298,7 +298,7 @@ static pg_status composite(const pg_image &in, const pg_se &se, const pg_image &
 }
 
 // ------------------------------------------------------------------ geodesy helpers
-static pg_status recon_se(int se, int rank, bool &conn8) {
+pg_status recon_se(int se, int rank, bool &conn8) {
   if (rank == 1 && se == PG_SE_SEGMENT_X_1D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_SQUARE_2D) { conn8 = true; return PG_OK; }
   if (rank == 2 && se == PG_SE_CROSS_2D) { conn8 = false; return PG_OK; }

@@ -129,6 +129,10 @@ void set_error(const std::string &msg);
 pg_status fail(pg_status st, const std::string &msg);
 pg_status cuda_status(cudaError_t e, const char *what);
 int num_sms();
+// Argument checks shared by the entry points (capi.cu): `in` -> `out` of one geometry and pixel
+// type in distinct buffers; the reconstruction's SE rule (sets conn8: 8-connected / 26 vs 4 / 6).
+pg_status check_in_out(const pg_image *in, const pg_image *out, const char *what);
+pg_status recon_se(int se, int rank, bool &conn8);
 
 #define PG_CUDA_TRY(expr, what)                                    \
   do {                                                             \

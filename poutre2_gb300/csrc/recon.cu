@@ -42,7 +42,8 @@ namespace pg {
 
 // tile side = threads per CTA: 64 (32 for 8-byte pixels, to keep the staged tile within the
 // 48 KB static shared-memory limit)
-template <typename T> __host__ __device__ constexpr int tile_side() { return sizeof(T) == 8 ? 32 : 64; }
+__host__ __device__ constexpr int tile_side_for(int elem_bytes) { return elem_bytes == 8 ? 32 : 64; }
+template <typename T> __host__ __device__ constexpr int tile_side() { return tile_side_for((int)sizeof(T)); }
 static constexpr int kMaxSweeps = 512;
 static constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;  // 4 s
 
@@ -1508,9 +1509,19 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 static_assert(sizeof(RCtl) <= kNoAllocFlagsOffset, "control block must fit below the flags");
 
+// Tiles of an H x W image in the no-alloc kernel (tile_side<T>() squares: 64, or 32 for 8-byte
+// pixels) and the most the fixed scratch holds (two flag words per tile above the control block).
+// The one place both numbers are computed: the entry point's shape check and the launch use it.
+static void noalloc_tiles(int elem_bytes, int64_t H, int64_t W, int64_t &ntiles, int64_t &max_tiles) {
+  const int64_t rt = tile_side_for(elem_bytes);
+  ntiles = ceil_div(H, rt) * ceil_div(W, rt);
+  max_tiles = (int64_t)((kNoAllocScratchBytes - kNoAllocFlagsOffset) / (2 * sizeof(unsigned)));
+}
+
 // Device address of g_noalloc_scratch, looked up once per device with that device current.
 // In host code the symbol name is only a host-side stand-in, so the kernel is given this
-// address instead.
+// address instead.  The address is kept for the life of the process: after cudaDeviceReset
+// (which destroys the context holding the array) this entry point must not be called again.
 static pg_status noalloc_scratch(void **out) {
   static std::mutex mu;
   static std::vector<void *> addr;  // indexed by device ordinal
@@ -1533,9 +1544,9 @@ static pg_status run_noalloc_t(RImg im, cudaStream_t s) {
   im.tiles_x = (int)ceil_div(im.W, RT);
   im.tiles_y = (int)ceil_div(im.H, RT);
   im.tile_begin = 0;
-  const int64_t ntiles = (int64_t)im.tiles_x * im.tiles_y;
+  int64_t ntiles = 0, max_tiles = 0;
+  noalloc_tiles((int)sizeof(T), im.H, im.W, ntiles, max_tiles);
   if (ntiles == 0) return PG_OK;
-  const int64_t max_tiles = (int64_t)((kNoAllocScratchBytes - kNoAllocFlagsOffset) / (2 * sizeof(unsigned)));
   if (ntiles > max_tiles)
     return fail(PG_ERR_INVALID_ARGUMENT, "pg_reconstruction_noalloc: the image needs " + std::to_string(ntiles) +
                                              " tiles of " + std::to_string(RT) + "x" + std::to_string(RT) +
@@ -1630,49 +1641,23 @@ int32_t pg_last_reconstruction_rounds(void) {
 // address; make it before any stream capture.
 pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker, const pg_image *mask, int32_t se,
                                     const pg_image *out, pg_stream_t stream) {
-  auto chk = [](const pg_image *a, const pg_image *b) -> pg_status {
-    if (!a || !b) return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_Reconstruct: null image descriptor");
-    if (a->rank < 1 || a->rank > 3 || b->rank != a->rank)
-      return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible size");
-    for (int i = 0; i < a->rank; ++i)
-      if (a->shape[i] != b->shape[i] || a->shape[i] < 0) return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible size");
-    if (!pg::elem_size(a->ptype)) return pg::fail(PG_ERR_UNSUPPORTED_PTYPE, "unsupported PTYPE");
-    if (a->ptype != b->ptype) return pg::fail(PG_ERR_INCOMPATIBLE, "t_Reconstruct incompatible types");
-    const int64_t n = pg::dims_of(*a).count();
-    if (n > 0 && (!a->data || !b->data)) return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_Reconstruct: null data pointer");
-    return PG_OK;
-  };
-  auto distinct = [](const pg_image *a, const pg_image *b) -> pg_status {
-    const int64_t n = pg::dims_of(*a).count();
-    const size_t bytes = (size_t)n * pg::elem_size(a->ptype);
-    const char *pa = static_cast<const char *>(a->data), *pb = static_cast<const char *>(b->data);
-    if (n > 0 && pa < pb + bytes && pb < pa + bytes)
-      return pg::fail(PG_ERR_ALIASING, "t_Reconstruct output must be != than input images");
-    return PG_OK;
-  };
-  PG_TRY(chk(marker, out));
-  PG_TRY(chk(mask, out));
-  {
-    // size limit of the fixed scratch, checked on the shape alone
-    const pg::Dims d = pg::dims_of(*mask);
-    const int rt = pg::elem_size(mask->ptype) == 8 ? 32 : 64;
-    const int64_t ntiles = pg::ceil_div(d.nz * d.ny, rt) * pg::ceil_div(d.nx, rt);
-    const int64_t max_tiles = (int64_t)((pg::kNoAllocScratchBytes - pg::kNoAllocFlagsOffset) / (2 * sizeof(unsigned)));
-    if (ntiles > max_tiles)
-      return pg::fail(PG_ERR_INVALID_ARGUMENT, "pg_reconstruction_noalloc: the image needs " + std::to_string(ntiles) +
-                                                   " tiles; the fixed scratch holds at most " +
-                                                   std::to_string(max_tiles));
-  }
-  PG_TRY(distinct(marker, out));
-  PG_TRY(distinct(mask, out));
+  // the checks of pg_reconstruction, in its order
+  PG_TRY(pg::check_in_out(marker, out, "t_Reconstruct"));
+  PG_TRY(pg::check_in_out(mask, out, "t_Reconstruct"));
   if (type != PG_RECONSTRUCT_ERODE && type != PG_RECONSTRUCT_DILATE)
     return pg::fail(PG_ERR_INVALID_ARGUMENT, "t_ReconstructionDispatchRectType unsupported reconstruction_type");
   bool conn8 = true;
-  const int rank = mask->rank;
-  if (rank == 1 && se == PG_SE_SEGMENT_X_1D) conn8 = true;
-  else if (rank == 2 && se == PG_SE_SQUARE_2D) conn8 = true;
-  else if (rank == 2 && se == PG_SE_CROSS_2D) conn8 = false;
-  else return pg::fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
+  PG_TRY(pg::recon_se(se, mask->rank, conn8));
+  // then the limits of this entry point
+  if (mask->rank == 3)
+    return pg::fail(PG_ERR_UNSUPPORTED_SE, "pg_reconstruction_noalloc: 1D and 2D images only (volumes need "
+                                           "pg_reconstruction)");
+  const pg::Dims d = pg::dims_of(*mask);
+  int64_t ntiles = 0, max_tiles = 0;
+  pg::noalloc_tiles(pg::elem_size(mask->ptype), d.nz * d.ny, d.nx, ntiles, max_tiles);
+  if (ntiles > max_tiles)
+    return pg::fail(PG_ERR_INVALID_ARGUMENT, "pg_reconstruction_noalloc: the image needs " + std::to_string(ntiles) +
+                                                 " tiles; the fixed scratch holds at most " + std::to_string(max_tiles));
   return pg::reconstruction_noalloc(type == PG_RECONSTRUCT_DILATE, conn8, *marker, *mask, *out,
                                     reinterpret_cast<cudaStream_t>(stream));
 }

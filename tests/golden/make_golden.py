@@ -185,7 +185,9 @@ def extract_compare(root: str):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <poutre2 source tree>")
+    root = sys.argv[1]
     cases = extract(root) + extract_compare(root)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(out, "w") as f:
