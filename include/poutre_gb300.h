@@ -49,7 +49,9 @@ typedef enum pg_status {
   PG_ERR_NOT_SQUARE = 6,        /* DilateY/ErodeY on a non-square image (the reference throws) */
   PG_ERR_CUDA = 7,              /* a CUDA runtime error (message in pg_last_error)          */
   PG_ERR_OUT_OF_MEMORY = 8,     /* a temporary could not be allocated                       */
-  PG_ERR_NOT_CONVERGED = 9      /* reconstruction hit its round cap or a device wait limit  */
+  PG_ERR_NOT_CONVERGED = 9,     /* reconstruction hit its round cap or a device wait limit  */
+  PG_ERR_SCALAR_TYPE = 10       /* a pg_scalar does not hold the pixel type the call needs   */
+                                /* ("unable to extract suitable type" in the reference)      */
 } pg_status;
 
 typedef enum pg_ptype {
@@ -89,6 +91,28 @@ typedef struct pg_image {
   int32_t rank;     /* 1, 2 or 3                                         */
   int64_t shape[3]; /* d0 .. d_{rank-1}; unused entries ignored          */
 } pg_image;
+
+/* One pixel value, held exactly: the role of poutre::ScalarTypeVariant
+ * (std::variant<pUINT8, pINT32, pINT64, pFLOAT, pDOUBLE>, include/poutre/base/types.hpp:529), plus
+ * uint16.  `ptype` names the member that is set.  A call taking a pg_scalar requires it to hold
+ * exactly the pixel type the reference's std::get<T> asks for (the image's, src/pixel_processing/
+ * arith.cpp:55; the output's for CompareImage's true / false values, compare.cpp:51-61), else it
+ * returns PG_ERR_SCALAR_TYPE where the reference's std::get throws std::bad_variant_access, which
+ * poutre2 rethrows as std::runtime_error "unable to extract suitable type" (arith.cpp:55-59,
+ * compare.cpp:50-62).  Every int64 value
+ * crosses the boundary exactly.  Floating-point values must be finite. */
+typedef struct pg_scalar {
+  int32_t ptype; /* pg_ptype of the member that holds the value */
+  int32_t reserved_;
+  union {
+    uint8_t u8;
+    uint16_t u16;
+    int32_t i32;
+    int64_t i64;
+    float f32;
+    double f64;
+  } v;
+} pg_scalar;
 
 /* Structuring element for the composite filters (opening/closing/gradient), which the
  * reference does not have: one of its SE vocabularies, selected by `kind`. */
@@ -185,24 +209,25 @@ PG_API pg_status pg_reconstruction(int32_t type, const pg_image *marker, const p
 
 /* poutre::geo::h_minima / h_maxima / h_concave / h_convex / dynamic_pseudo_opening /
  * dynamic_pseudo_closing(const IInterface&, const ScalarTypeVariant& h, se::Common_NL_SE, IInterface&),
- * include/poutre/geodesy/extrema.hpp:33-64.  `h` must be exactly representable in the pixel type
- * (the reference requires the variant to hold the pixel type, src/pixel_processing/arith.cpp:55). */
-PG_API pg_status pg_h_minima(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_h_maxima(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_h_concave(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_h_convex(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_dynamic_pseudo_opening(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_dynamic_pseudo_closing(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+ * include/poutre/geodesy/extrema.hpp:33-64.  `h` must hold the image's pixel type, as the reference's
+ * ScalarTypeVariant must (src/pixel_processing/arith.cpp:55); else PG_ERR_SCALAR_TYPE. */
+PG_API pg_status pg_h_minima(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_maxima(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_concave(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_convex(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dynamic_pseudo_opening(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_dynamic_pseudo_closing(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
 
 /* Binary regional maxima of the h-maxima transform, one fused launch: out(u8) = 255 where
  * in > h_maxima(in) else 0, i.e. h_maxima followed by CompareImage(in, CompOpSup, rec, 255, 0)
  * (include/poutre/pixel_processing/compare.hpp:69). `out` is a u8 image of in's shape. */
-PG_API pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t common_se, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_h_maxima_binary(const pg_image *in, const pg_scalar *h, int32_t common_se, const pg_image *out, pg_stream_t stream);
 
 /* Ragged batch of the binary h-maxima: n independent 2D images of any sizes in ONE persistent
  * launch (tile table over all images).  ins[i]/outs[i] are device images (outs u8); volumes are
  * taken one after the other by the 3D route of pg_reconstruction. */
-PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t common_se,
+PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, const pg_scalar *h,
+                                          int32_t common_se,
                                    pg_stream_t stream);
 
 /* A prepared ragged batch of the binary h-maxima (no reference counterpart): the image and tile
@@ -216,7 +241,7 @@ PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *o
  * pg_batch_plan_set_config pins the configuration: tile 32 or 64 (64 only for pixels of at most
  * 4 bytes), sweeps >= 1 (a tile that reaches the cap yields and is revisited next round). */
 typedef struct pg_batch_plan pg_batch_plan;
-PG_API pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, double h,
+PG_API pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, const pg_scalar *h,
                                                int32_t common_se, int32_t autotune, pg_batch_plan **plan,
                                                pg_stream_t stream);
 PG_API pg_status pg_batch_plan_run(pg_batch_plan *plan, pg_stream_t stream);
@@ -237,9 +262,9 @@ PG_API pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_
 
 /* poutre::ArithSaturatedSubConstant / ArithSaturatedAddConstant (src/pixel_processing/arith.cpp:471):
  * integers clamp to the pixel type's range, floating point is the plain IEEE result (as for the
- * saturated image arithmetic below); `v` must be representable in the pixel type. */
-PG_API pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
-PG_API pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t stream);
+ * saturated image arithmetic below); `v` must hold the image's pixel type (PG_ERR_SCALAR_TYPE). */
+PG_API pg_status pg_sat_sub_constant(const pg_image *in, const pg_scalar *v, const pg_image *out, pg_stream_t stream);
+PG_API pg_status pg_sat_add_constant(const pg_image *in, const pg_scalar *v, const pg_image *out, pg_stream_t stream);
 
 /* ---------------------------------------------------------------- pixel processing */
 /* poutre::CompOpType (include/poutre/base/types.hpp:443-452), same values. */
@@ -253,11 +278,11 @@ typedef enum {
 } pg_comp_op;
 
 /* One operand of CompareImage: an image of the input's geometry (image != NULL) or the scalar
- * `value` (the reference's ScalarTypeVariant; it must be representable in the operand's pixel
- * type: integral and in range for integer pixels). */
+ * `value` (the reference's ScalarTypeVariant): the comparand holds the input's pixel type, the
+ * true / false values the output's (compare.cpp:51-61), else PG_ERR_SCALAR_TYPE. */
 typedef struct {
   const pg_image *image;
-  double value;
+  pg_scalar value;
 } pg_operand;
 
 /* poutre::ArithInvertImage / ArithSupImage / ArithInfImage / ArithSaturatedAddImage /

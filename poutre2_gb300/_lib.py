@@ -16,7 +16,7 @@ PG_OK = 0
 STATUS_NAMES = {
     0: "PG_OK", 1: "PG_ERR_INVALID_ARGUMENT", 2: "PG_ERR_UNSUPPORTED_PTYPE", 3: "PG_ERR_UNSUPPORTED_SE",
     4: "PG_ERR_INCOMPATIBLE", 5: "PG_ERR_ALIASING", 6: "PG_ERR_NOT_SQUARE", 7: "PG_ERR_CUDA",
-    8: "PG_ERR_OUT_OF_MEMORY", 9: "PG_ERR_NOT_CONVERGED",
+    8: "PG_ERR_OUT_OF_MEMORY", 9: "PG_ERR_NOT_CONVERGED", 10: "PG_ERR_SCALAR_TYPE",
 }
 
 # every symbol include/poutre_gb300.h declares
@@ -52,9 +52,61 @@ class PgImage(ctypes.Structure):
                 ("shape", ctypes.c_int64 * 3)]
 
 
+class _ScalarValue(ctypes.Union):
+    _fields_ = [("u8", ctypes.c_uint8), ("u16", ctypes.c_uint16), ("i32", ctypes.c_int32), ("i64", ctypes.c_int64),
+                ("f32", ctypes.c_float), ("f64", ctypes.c_double)]
+
+
+class PgScalar(ctypes.Structure):
+    """pg_scalar: one pixel value held exactly, tagged with its pixel type (ScalarTypeVariant)."""
+    _fields_ = [("ptype", ctypes.c_int32), ("reserved_", ctypes.c_int32), ("v", _ScalarValue)]
+
+
+# pg_ptype -> (union member, lowest, highest); floating-point members have no bounds here
+_SCALAR_MEMBER = {4: ("u8", 0, 255), 128: ("u16", 0, 65535), 8: ("i32", -2**31, 2**31 - 1),
+                  32: ("i64", -2**63, 2**63 - 1), 16: ("f32", None, None), 64: ("f64", None, None)}
+_NUMPY_PTYPE = {"uint8": 4, "uint16": 128, "int32": 8, "int64": 32, "float32": 16, "float64": 64}
+
+
+def scalar(ptype: int, value) -> PgScalar:
+    """The pg_scalar a call receives for `value`.
+
+    A numpy scalar keeps its own type (``np.int32(5)`` holds INT32), and the library then checks it
+    against the pixel type as poutre2's ``std::get`` checks a ScalarTypeVariant (PG_ERR_SCALAR_TYPE
+    on a mismatch).  A Python int or float is taken as pixel type `ptype`: an integer type needs an
+    integral value in its range (Python ints stay exact up to the int64 limits), else
+    PoutreError(PG_ERR_SCALAR_TYPE) is raised here."""
+    import numbers
+
+    import numpy as np
+    if isinstance(value, np.generic):
+        pt = _NUMPY_PTYPE.get(value.dtype.name)
+        if pt is None:
+            raise PoutreError(10, f"no pixel type holds a {value.dtype.name} scalar")
+        value = value.item()
+    else:
+        pt = int(ptype)
+    if pt not in _SCALAR_MEMBER:
+        raise PoutreError(2, f"unsupported PTYPE {pt}")
+    member, lo, hi = _SCALAR_MEMBER[pt]
+    s = PgScalar()
+    s.ptype = pt
+    if lo is None:
+        if isinstance(value, bool) or not isinstance(value, numbers.Real):
+            raise PoutreError(10, f"{value!r} is not a value of a floating-point pixel type")
+        setattr(s.v, member, float(value))
+        return s
+    if isinstance(value, float) and value.is_integer():
+        value = int(value)
+    if isinstance(value, bool) or not isinstance(value, numbers.Integral) or not lo <= int(value) <= hi:
+        raise PoutreError(10, f"{value!r} is not a value of the pixel type ({member})")
+    setattr(s.v, member, int(value))
+    return s
+
+
 class PgOperand(ctypes.Structure):
     """pg_operand: an image (``image`` set) or the scalar ``value`` of CompareImage."""
-    _fields_ = [("image", ctypes.POINTER(PgImage)), ("value", ctypes.c_double)]
+    _fields_ = [("image", ctypes.POINTER(PgImage)), ("value", PgScalar)]
 
 
 class PgSE(ctypes.Structure):
@@ -79,9 +131,10 @@ def load(path: str | None = None):
         L = ctypes.CDLL(p)
         img = ctypes.POINTER(PgImage)
         se = ctypes.POINTER(PgSE)
-        I32, I64, D, VP = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+        I32, I64, VP = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p
         i32p = ctypes.POINTER(ctypes.c_int32)
         fp = ctypes.c_void_p
+        D = ctypes.POINTER(PgScalar)  # the scalar arguments (h, v): const pg_scalar *
         sig = {
             "pg_erode": [img, I32, I32, img, VP], "pg_dilate": [img, I32, I32, img, VP],
             "pg_erode_compound": [img, I32, I32, img, VP], "pg_dilate_compound": [img, I32, I32, img, VP],

@@ -103,20 +103,29 @@ static int se_rank(int se) {
   }
 }
 
-// integer pixel scalar must be an exact value of the pixel type (ScalarTypeVariant holds
-// exactly the image's type, src/pixel_processing/arith.cpp:55)
-static pg_status check_scalar(int ptype, double v, const char *what) {
-  if (!std::isfinite(v)) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": non-finite scalar");
-  double lo = 0, hi = 0;
-  switch (ptype) {
-    case PG_PTYPE_U8: lo = 0; hi = 255; break;
-    case PG_PTYPE_U16: lo = 0; hi = 65535; break;
-    case PG_PTYPE_I32: lo = -2147483648.0; hi = 2147483647.0; break;
-    case PG_PTYPE_I64: lo = -9223372036854775808.0; hi = 9223372036854774784.0; break;
-    default: return PG_OK;
+// A ScalarTypeVariant must hold exactly the pixel type the reference's std::get<T> asks for
+// (src/pixel_processing/arith.cpp:55, compare.cpp:51-61); where it does not, poutre2 catches
+// std::bad_variant_access and throws "unable to extract suitable type".  Floating-point values must
+// also be finite.
+static const char *ptype_name(int pt) {
+  switch (pt) {
+    case PG_PTYPE_U8: return "UINT8";
+    case PG_PTYPE_U16: return "UINT16";
+    case PG_PTYPE_I32: return "INT32";
+    case PG_PTYPE_I64: return "INT64";
+    case PG_PTYPE_F32: return "FLOAT";
+    case PG_PTYPE_F64: return "DOUBLE";
+    default: return "undefined";
   }
-  if (v != std::floor(v) || v < lo || v > hi)
-    return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": scalar is not a value of the pixel type");
+}
+
+static pg_status check_scalar(int ptype, const pg_scalar *v, const char *what) {
+  if (!v) return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": null scalar");
+  if (v->ptype != ptype)
+    return fail(PG_ERR_SCALAR_TYPE, std::string(what) + " unable to extract suitable type from the scalar (it holds " +
+                                        ptype_name(v->ptype) + ", the pixel type is " + ptype_name(ptype) + ")");
+  if ((ptype == PG_PTYPE_F32 && !std::isfinite(v->v.f32)) || (ptype == PG_PTYPE_F64 && !std::isfinite(v->v.f64)))
+    return fail(PG_ERR_INVALID_ARGUMENT, std::string(what) + ": non-finite scalar");
   return PG_OK;
 }
 
@@ -310,7 +319,7 @@ pg_status recon_se(int se, int rank, bool &conn8) {
   return fail(PG_ERR_UNSUPPORTED_SE, "t_ReconstructionDispatchNl unsupported nl_static");
 }
 
-static pg_status h_recon(const pg_image *in, double h, int se, const pg_image *out, bool maxima, cudaStream_t s) {
+static pg_status h_recon(const pg_image *in, const pg_scalar &h, int se, const pg_image *out, bool maxima, cudaStream_t s) {
   ReconRequest rq;
   PG_TRY(recon_se(se, in->rank, rq.conn8));
   rq.dilate = maxima;
@@ -342,7 +351,7 @@ static pg_status label_extrema(const pg_image *in, int32_t se, const pg_image *o
   pg_image r = *in, e = *in;
   r.data = rec.ptr;
   e.data = ext.ptr;
-  PG_TRY(h_recon(in, 1.0, se, &r, maxima, s));  // h_maxima / h_minima with h = 1
+  PG_TRY(h_recon(in, scalar_of(in->ptype, 1), se, &r, maxima, s));  // h_maxima / h_minima with h = 1
   // h_convex = sat_sub(f, h_maxima(f)), h_concave = sat_sub(h_minima(f), f) (extrema.cpp:51-73)
   PG_TRY(maxima ? launch_sat_sub_image(*in, r, e, s) : launch_sat_sub_image(r, *in, e, s));
   return launch_label(e, se, *out, false, nb_labels, s);
@@ -483,38 +492,38 @@ pg_status pg_reconstruction(int32_t type, const pg_image *marker, const pg_image
   return launch_reconstruction(marker, mask, out, 1, rq, STREAM(s));
 }
 
-pg_status pg_h_maxima(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_h_maxima(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "h_maxima"));
   PG_TRY(check_scalar(in->ptype, h, "h_maxima"));
-  return h_recon(in, h, se, out, true, STREAM(s));
+  return h_recon(in, *h, se, out, true, STREAM(s));
 }
-pg_status pg_h_minima(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_h_minima(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "h_minima"));
   PG_TRY(check_scalar(in->ptype, h, "h_minima"));
-  return h_recon(in, h, se, out, false, STREAM(s));
+  return h_recon(in, *h, se, out, false, STREAM(s));
 }
-pg_status pg_h_convex(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_h_convex(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "h_convex"));
   PG_TRY(check_scalar(in->ptype, h, "h_convex"));
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(*in).count() * elem_size(in->ptype), STREAM(s)));
   pg_image t = *in;
   t.data = tmp.ptr;
-  PG_TRY(h_recon(in, h, se, &t, true, STREAM(s)));
+  PG_TRY(h_recon(in, *h, se, &t, true, STREAM(s)));
   return launch_sat_sub_image(*in, t, *out, STREAM(s));  // sat_sub(f, h_maxima(f)) (extrema.cpp:63-73)
 }
-pg_status pg_h_concave(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_h_concave(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "h_concave"));
   PG_TRY(check_scalar(in->ptype, h, "h_concave"));
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(*in).count() * elem_size(in->ptype), STREAM(s)));
   pg_image t = *in;
   t.data = tmp.ptr;
-  PG_TRY(h_recon(in, h, se, &t, false, STREAM(s)));
+  PG_TRY(h_recon(in, *h, se, &t, false, STREAM(s)));
   return launch_sat_sub_image(t, *in, *out, STREAM(s));  // sat_sub(h_minima(f), f) (extrema.cpp:51-61)
 }
 
-static pg_status dyn_pseudo(const pg_image *in, double h, int se, const pg_image *out, bool opening, cudaStream_t s) {
+static pg_status dyn_pseudo(const pg_image *in, const pg_scalar &h, int se, const pg_image *out, bool opening, cudaStream_t s) {
   Scratch a, b;
   const size_t bytes = (size_t)dims_of(*in).count() * elem_size(in->ptype);
   PG_TRY(a.alloc(bytes, s));
@@ -529,15 +538,15 @@ static pg_status dyn_pseudo(const pg_image *in, double h, int se, const pg_image
   rq.dilate = opening;
   return launch_reconstruction(&mk, in, out, 1, rq, s);
 }
-pg_status pg_dynamic_pseudo_opening(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_dynamic_pseudo_opening(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "dynamic_pseudo_opening"));
   PG_TRY(check_scalar(in->ptype, h, "dynamic_pseudo_opening"));
-  return dyn_pseudo(in, h, se, out, true, STREAM(s));
+  return dyn_pseudo(in, *h, se, out, true, STREAM(s));
 }
-pg_status pg_dynamic_pseudo_closing(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_dynamic_pseudo_closing(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "dynamic_pseudo_closing"));
   PG_TRY(check_scalar(in->ptype, h, "dynamic_pseudo_closing"));
-  return dyn_pseudo(in, h, se, out, false, STREAM(s));
+  return dyn_pseudo(in, *h, se, out, false, STREAM(s));
 }
 
 static pg_status check_binary_out(const pg_image *in, const pg_image *out, const char *what) {
@@ -549,7 +558,7 @@ static pg_status check_binary_out(const pg_image *in, const pg_image *out, const
   return PG_OK;
 }
 
-pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t se, const pg_image *out, pg_stream_t s) {
+pg_status pg_h_maxima_binary(const pg_image *in, const pg_scalar *h, int32_t se, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_binary_out(in, out, "h_maxima_binary"));
   PG_TRY(check_scalar(in->ptype, h, "h_maxima_binary"));
   ReconRequest rq;
@@ -557,11 +566,11 @@ pg_status pg_h_maxima_binary(const pg_image *in, double h, int32_t se, const pg_
   rq.dilate = true;
   rq.init = INIT_SAT_CONST;
   rq.epi = EPI_BINARY_SUP;
-  rq.h = h;
+  rq.h = *h;
   return launch_reconstruction(nullptr, in, out, 1, rq, STREAM(s));
 }
 
-pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t se,
+pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, int32_t n, const pg_scalar *h, int32_t se,
                                    pg_stream_t s) {
   if (n < 0 || (n > 0 && (!ins || !outs))) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch: bad image arrays");
   if (n == 0) return PG_OK;
@@ -576,11 +585,11 @@ pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *outs, in
   rq.dilate = true;
   rq.init = INIT_SAT_CONST;
   rq.epi = EPI_BINARY_SUP;
-  rq.h = h;
+  rq.h = *h;
   return launch_reconstruction(nullptr, ins, outs, n, rq, STREAM(s));
 }
 
-pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, double h, int32_t se,
+pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *outs, int32_t n, const pg_scalar *h, int32_t se,
                                         int32_t autotune, pg_batch_plan **plan, pg_stream_t s) {
   if (!plan) return fail(PG_ERR_INVALID_ARGUMENT, "null plan pointer");
   *plan = nullptr;
@@ -595,7 +604,7 @@ pg_status pg_h_maxima_binary_batch_plan(const pg_image *ins, const pg_image *out
   if (ins[0].rank == 3) return fail(PG_ERR_INVALID_ARGUMENT, "h_maxima_binary_batch_plan: images of rank 1 or 2");
   bool conn8 = true;
   PG_TRY(recon_se(se, ins[0].rank, conn8));
-  return create_batch_plan(ins, outs, n, h, conn8, autotune != 0, STREAM(s), plan);
+  return create_batch_plan(ins, outs, n, *h, conn8, autotune != 0, STREAM(s), plan);
 }
 pg_status pg_batch_plan_run(pg_batch_plan *plan, pg_stream_t s) {
   if (!plan) return fail(PG_ERR_INVALID_ARGUMENT, "null plan");
@@ -640,15 +649,15 @@ pg_status pg_leveling(const pg_image *ref, const pg_image *marker, int32_t se, c
 }
 
 // ---------------------------------------------------------------- pixel processing
-pg_status pg_sat_sub_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t s) {
+pg_status pg_sat_sub_constant(const pg_image *in, const pg_scalar *v, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "ArithSaturatedSubConstant"));
   PG_TRY(check_scalar(in->ptype, v, "ArithSaturatedSubConstant"));
-  return launch_sat_const(*in, v, false, *out, STREAM(s));
+  return launch_sat_const(*in, *v, false, *out, STREAM(s));
 }
-pg_status pg_sat_add_constant(const pg_image *in, double v, const pg_image *out, pg_stream_t s) {
+pg_status pg_sat_add_constant(const pg_image *in, const pg_scalar *v, const pg_image *out, pg_stream_t s) {
   PG_TRY(check_in_out(in, out, "ArithSaturatedAddConstant"));
   PG_TRY(check_scalar(in->ptype, v, "ArithSaturatedAddConstant"));
-  return launch_sat_const(*in, v, true, *out, STREAM(s));
+  return launch_sat_const(*in, *v, true, *out, STREAM(s));
 }
 
 // ---------------------------------------------------------------- pixel processing
@@ -716,9 +725,9 @@ pg_status pg_compare_image(const pg_image *in, int32_t op, const pg_operand *com
       if (!same_geometry(*im, *out)) return fail(PG_ERR_INCOMPATIBLE, "CompareImage images have not compatible sizes");
       if (im->ptype != pt) return fail(PG_ERR_INCOMPATIBLE, std::string("CompareImage ") + names[k] + " downcast fail");
       if (partial_overlap(*im, *out)) return fail(PG_ERR_ALIASING, "CompareImage output overlaps an input partially");
-      ops[k] = CompareOperand{im->data, 0.0};
+      ops[k] = CompareOperand{im->data, pg_scalar{}};
     } else {
-      PG_TRY(check_scalar(pt, src[k]->value,
+      PG_TRY(check_scalar(pt, &src[k]->value,
                           (std::string("CompareImage unable to extract suitable type from ") + names[k]).c_str()));
       ops[k] = CompareOperand{nullptr, src[k]->value};
     }

@@ -178,6 +178,36 @@ struct Scratch {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// The value of a pg_scalar as pixel type T.  The entry points check that the scalar holds T's own
+// pg_ptype (check_scalar), so this reads the member that holds the value and converts nothing.
+template <typename T> inline T scalar_as(const pg_scalar &s) {
+  switch (s.ptype) {
+    case PG_PTYPE_U8: return static_cast<T>(s.v.u8);
+    case PG_PTYPE_U16: return static_cast<T>(s.v.u16);
+    case PG_PTYPE_I32: return static_cast<T>(s.v.i32);
+    case PG_PTYPE_I64: return static_cast<T>(s.v.i64);
+    case PG_PTYPE_F32: return static_cast<T>(s.v.f32);
+    case PG_PTYPE_F64: return static_cast<T>(s.v.f64);
+    default: return T(0);
+  }
+}
+
+// A pg_scalar holding `v` as pixel type `ptype` (for constants the library itself passes, e.g. h = 1).
+inline pg_scalar scalar_of(int ptype, int64_t v) {
+  pg_scalar s{};
+  s.ptype = ptype;
+  switch (ptype) {
+    case PG_PTYPE_U8: s.v.u8 = (uint8_t)v; break;
+    case PG_PTYPE_U16: s.v.u16 = (uint16_t)v; break;
+    case PG_PTYPE_I32: s.v.i32 = (int32_t)v; break;
+    case PG_PTYPE_I64: s.v.i64 = v; break;
+    case PG_PTYPE_F32: s.v.f32 = (float)v; break;
+    case PG_PTYPE_F64: s.v.f64 = (double)v; break;
+    default: break;
+  }
+  return s;
+}
+
 // Dispatch over pixel types.
 #define PG_DISPATCH_PTYPE(pt, T, ...)                                        \
   switch (pt) {                                                              \
@@ -239,7 +269,7 @@ int take_label_status();
 int take_rect_status();  // device status of the fused square kernel since the last call (0: none)
 pg_status launch_copy(const pg_image &in, const pg_image &out, cudaStream_t s);
 pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
-pg_status launch_sat_const(const pg_image &in, double v, bool add, const pg_image &out, cudaStream_t s);
+pg_status launch_sat_const(const pg_image &in, const pg_scalar &v, bool add, const pg_image &out, cudaStream_t s);
 pg_status launch_sat_sub_image(const pg_image &a, const pg_image &b, const pg_image &out, cudaStream_t s);
 
 // pixel.cu: ArithInf/Sup/SaturatedAdd/SaturatedSub/Invert image, CompareImage, ConvertInto
@@ -247,12 +277,12 @@ enum PixelOp { PX_INF = 0, PX_SUP = 1, PX_SADD = 2, PX_SSUB = 3, PX_NEG = 4 };
 pg_status launch_pixel_arith(int op, const pg_image &a, const pg_image *b, const pg_image &out, cudaStream_t s);
 struct CompareOperand {
   const void *data;  // image pixels, or nullptr for the scalar `value`
-  double value;
+  pg_scalar value;
 };
 pg_status launch_compare(const pg_image &in, int op, const CompareOperand &comp, const CompareOperand &vt,
                          const CompareOperand &vf, const pg_image &out, cudaStream_t s);
 pg_status launch_convert(const pg_image &in, const pg_image &out, cudaStream_t s);
-pg_status launch_dyn_pseudo_marker(const pg_image &f, const pg_image &ext, double h, bool opening, const pg_image &out,
+pg_status launch_dyn_pseudo_marker(const pg_image &f, const pg_image &ext, const pg_scalar &h, bool opening, const pg_image &out,
                                    cudaStream_t s);
 
 // Reconstruction family (recon.cu)
@@ -265,7 +295,7 @@ struct ReconRequest {
   int init = INIT_MARKER;
   int mask_mode = MASK_PLAIN;
   int epi = EPI_NONE;
-  double h = 0.0;         // INIT_SAT_CONST constant
+  pg_scalar h{};          // INIT_SAT_CONST constant (holds the image's pixel type)
 };
 pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, const pg_image *outs, int n_images,
                                 const ReconRequest &rq, cudaStream_t s);
@@ -274,7 +304,7 @@ pg_status launch_reconstruction(const pg_image *markers, const pg_image *masks, 
 pg_status launch_reconstruction3d(const pg_image *marker, const pg_image &mask, const pg_image &out,
                                   const ReconRequest &rq, cudaStream_t s);
 
-pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, double h, bool conn8, bool autotune,
+pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, const pg_scalar &h, bool conn8, bool autotune,
                             cudaStream_t s, pg_batch_plan **out_plan);
 pg_status run_batch_plan(pg_batch_plan *p, cudaStream_t s);
 void destroy_batch_plan(pg_batch_plan *p);

@@ -133,8 +133,8 @@ __global__ void __launch_bounds__(kPThreads)
   }
 }
 
-template <typename T> Operand<T> operand_of(const void *img, double v) {
-  return Operand<T>{static_cast<const T *>(img), static_cast<T>(v)};
+template <typename T> Operand<T> operand_of(const void *img, const pg_scalar &v) {
+  return Operand<T>{static_cast<const T *>(img), img ? T(0) : scalar_as<T>(v)};
 }
 
 }  // namespace

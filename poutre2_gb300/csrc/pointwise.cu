@@ -73,12 +73,12 @@ pg_status launch_sub(const pg_image &a, const pg_image &b, const pg_image &out, 
   return cuda_status(cudaGetLastError(), "difference kernel launch");
 }
 
-pg_status launch_sat_const(const pg_image &in, double v, bool add, const pg_image &out, cudaStream_t s) {
+pg_status launch_sat_const(const pg_image &in, const pg_scalar &v, bool add, const pg_image &out, cudaStream_t s) {
   const int64_t n = dims_of(in).count();
   if (n == 0) return PG_OK;
   PG_DISPATCH_PTYPE(in.ptype, T, {
     k_sat_const<T><<<grid_for(n), 256, 0, s>>>(static_cast<const T *>(in.data), static_cast<T *>(out.data), n,
-                                              static_cast<T>(v), add);
+                                              scalar_as<T>(v), add);
   });
   return cuda_status(cudaGetLastError(), "saturated constant kernel launch");
 }
@@ -93,13 +93,13 @@ pg_status launch_sat_sub_image(const pg_image &a, const pg_image &b, const pg_im
   return cuda_status(cudaGetLastError(), "saturated difference kernel launch");
 }
 
-pg_status launch_dyn_pseudo_marker(const pg_image &f, const pg_image &ext, double h, bool opening,
+pg_status launch_dyn_pseudo_marker(const pg_image &f, const pg_image &ext, const pg_scalar &h, bool opening,
                                    const pg_image &out, cudaStream_t s) {
   const int64_t n = dims_of(f).count();
   if (n == 0) return PG_OK;
   PG_DISPATCH_PTYPE(f.ptype, T, {
     k_dyn_marker<T><<<grid_for(n), 256, 0, s>>>(static_cast<const T *>(f.data), static_cast<const T *>(ext.data),
-                                               static_cast<T *>(out.data), n, static_cast<T>(h), opening);
+                                               static_cast<T *>(out.data), n, scalar_as<T>(h), opening);
   });
   return cuda_status(cudaGetLastError(), "pseudo-dynamic marker kernel launch");
 }

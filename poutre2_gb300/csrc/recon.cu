@@ -1268,7 +1268,7 @@ static pg_status run_t(std::vector<RImg> &imgs, const ReconRequest &rq, bool bin
   P.init = rq.init;
   P.mask_mode = rq.mask_mode;
   P.epi = rq.epi;
-  P.h = static_cast<T>(rq.h);
+  P.h = scalar_as<T>(rq.h);
   return launch_recon<T, SUP, CONN8, RT>(P, base, s, nullptr);
 }
 
@@ -1327,7 +1327,7 @@ struct pg_batch_plan {
   int device = 0;
   int ptype = 0;
   bool conn8 = true;
-  double h = 0;
+  pg_scalar h{};
   void *scratch = nullptr;  // control block | flags (sized for the finest tiling) | recon buffers
   size_t clear_bytes = 0;
   pg::PlanTable t64, t32;
@@ -1351,7 +1351,7 @@ static pg_status plan_launch_t(pg_batch_plan &p, int sweeps, cudaStream_t s, int
   P.init = INIT_SAT_CONST;
   P.mask_mode = MASK_PLAIN;
   P.epi = EPI_BINARY_SUP;
-  P.h = static_cast<T>(p.h);
+  P.h = scalar_as<T>(p.h);
   PG_CUDA_TRY(cudaMemsetAsync(p.scratch, 0, p.clear_bytes, s), "clear batch work area");
   return launch_recon<T, true, CONN8, RT>(P, static_cast<char *>(p.scratch), s, grid_out);
 }
@@ -1391,7 +1391,7 @@ struct TuneKey {
   }
 };
 
-pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, double h, bool conn8, bool autotune,
+pg_status create_batch_plan(const pg_image *ins, const pg_image *outs, int n, const pg_scalar &h, bool conn8, bool autotune,
                             cudaStream_t s, pg_batch_plan **out_plan) {
   auto plan = std::make_unique<pg_batch_plan>();
   PG_CUDA_TRY(cudaGetDevice(&plan->device), "cudaGetDevice");

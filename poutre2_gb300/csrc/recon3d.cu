@@ -105,7 +105,7 @@ pg_status recon3d_t(const pg_image *marker, const pg_image &mask, const pg_image
   int *d_flag = static_cast<int *>(flag.ptr);
   k_r3_prep<T, SUP><<<flat_grid(n), 256, 0, s>>>(ref, marker ? static_cast<const T *>(marker->data) : nullptr,
                                                  own_mask ? static_cast<T *>(emask.ptr) : nullptr, a, n, rq.init,
-                                                 rq.mask_mode, static_cast<T>(rq.h));
+                                                 rq.mask_mode, scalar_as<T>(rq.h));
   PG_CUDA_TRY(cudaGetLastError(), "3D reconstruction prep launch");
   const dim3 block(32, 8), grid((unsigned)ceil_div(d.nx, 32), (unsigned)ceil_div(d.ny, 8), (unsigned)d.nz);
   const int64_t max_steps = n + kStepBatch + 1;

@@ -44,7 +44,8 @@ def Reconstruction(rect_type, i_marker, i_mask, nl_static, o_img, check=None):
 
 def _extrema(name, i_img, pvalue, nl_static, o_img, check):
     di, do = descriptor(i_img, "input"), descriptor(o_img, "output")
-    _lib.call(name, ctypes.byref(di), float(pvalue), int(Common_NL_SE(nl_static)), ctypes.byref(do), _stream())
+    h = _lib.scalar(di.ptype, pvalue)
+    _lib.call(name, ctypes.byref(di), ctypes.byref(h), int(Common_NL_SE(nl_static)), ctypes.byref(do), _stream())
     _post(check)
 
 
@@ -84,7 +85,8 @@ def h_maxima_binary_batch(imgs: Sequence[torch.Tensor], pvalue, nl_static, outs:
         raise _lib.PoutreError(1, "h_maxima_binary_batch: as many outputs as inputs are needed")
     ins = (_lib.PgImage * n)(*[descriptor(t, "input") for t in imgs])
     ous = (_lib.PgImage * n)(*[descriptor(t, "output") for t in outs])
-    _lib.call("pg_h_maxima_binary_batch", ins, ous, n, float(pvalue), int(Common_NL_SE(nl_static)), _stream())
+    h = _lib.scalar(ins[0].ptype if n else 4, pvalue)
+    _lib.call("pg_h_maxima_binary_batch", ins, ous, n, ctypes.byref(h), int(Common_NL_SE(nl_static)), _stream())
     _post(check)
 
 
@@ -127,7 +129,8 @@ class HMaximaBinaryBatch:
         ins = (_lib.PgImage * n)(*[descriptor(t, "input") for t in imgs])
         ous = (_lib.PgImage * n)(*[descriptor(t, "output") for t in outs])
         self._plan = ctypes.c_void_p()
-        _lib.call("pg_h_maxima_binary_batch_plan", ins, ous, n, float(pvalue), int(Common_NL_SE(nl_static)),
+        h = _lib.scalar(ins[0].ptype, pvalue)
+        _lib.call("pg_h_maxima_binary_batch_plan", ins, ous, n, ctypes.byref(h), int(Common_NL_SE(nl_static)),
                   int(bool(autotune)), ctypes.byref(self._plan), _stream())
 
     def run(self, check=False):

@@ -65,13 +65,15 @@ def ArithSaturatedSubImage(i_img1: torch.Tensor, i_img2: torch.Tensor, o_img: to
 def ArithSaturatedAddConstant(i_img: torch.Tensor, pvalue, o_img: torch.Tensor) -> None:
     """poutre::ArithSaturatedAddConstant (src/pixel_processing/arith.cpp)."""
     a, o = descriptor(i_img, "input"), descriptor(o_img, "output")
-    _lib.call("pg_sat_add_constant", ctypes.byref(a), float(pvalue), ctypes.byref(o), _lib.current_stream())
+    v = _lib.scalar(a.ptype, pvalue)
+    _lib.call("pg_sat_add_constant", ctypes.byref(a), ctypes.byref(v), ctypes.byref(o), _lib.current_stream())
 
 
 def ArithSaturatedSubConstant(i_img: torch.Tensor, pvalue, o_img: torch.Tensor) -> None:
     """poutre::ArithSaturatedSubConstant (src/pixel_processing/arith.cpp:471)."""
     a, o = descriptor(i_img, "input"), descriptor(o_img, "output")
-    _lib.call("pg_sat_sub_constant", ctypes.byref(a), float(pvalue), ctypes.byref(o), _lib.current_stream())
+    v = _lib.scalar(a.ptype, pvalue)
+    _lib.call("pg_sat_sub_constant", ctypes.byref(a), ctypes.byref(v), ctypes.byref(o), _lib.current_stream())
 
 
 def CompareImage(i_img: torch.Tensor, compOpType, i_comp, i_valtrue, i_valfalse, o_img: torch.Tensor) -> None:
@@ -81,15 +83,17 @@ def CompareImage(i_img: torch.Tensor, compOpType, i_comp, i_valtrue, i_valfalse,
     device image of the input's shape or a Python scalar."""
     keep = []
 
-    def operand(v, what):
+    a, o = descriptor(i_img, "input"), descriptor(o_img, "output")
+
+    def operand(v, what, ptype):
         if isinstance(v, torch.Tensor):
             d = descriptor(v, what)
             keep.append(d)
-            return _lib.PgOperand(ctypes.pointer(d), 0.0)
-        return _lib.PgOperand(None, float(v))
+            return _lib.PgOperand(ctypes.pointer(d), _lib.PgScalar())
+        return _lib.PgOperand(None, _lib.scalar(ptype, v))
 
-    c, t, f = operand(i_comp, "i_comp"), operand(i_valtrue, "i_valtrue"), operand(i_valfalse, "i_valfalse")
-    a, o = descriptor(i_img, "input"), descriptor(o_img, "output")
+    c = operand(i_comp, "i_comp", a.ptype)
+    t, f = operand(i_valtrue, "i_valtrue", o.ptype), operand(i_valfalse, "i_valfalse", o.ptype)
     _lib.call("pg_compare_image", ctypes.byref(a), int(CompOpType(compOpType)), ctypes.byref(c), ctypes.byref(t),
               ctypes.byref(f), ctypes.byref(o), _lib.current_stream())
 

@@ -96,12 +96,12 @@ int main(int argc, char **argv) {
         if (op == "low_leveling") geo::low_leveling(a, b, se_of(sen), o);
         else if (op == "high_leveling") geo::high_leveling(a, b, se_of(sen), o);
         else geo::leveling(a, b, se_of(sen), o);
-      } else if (op == "h_minima") geo::h_minima(a, param, se_of(sen), o);
-      else if (op == "h_maxima") geo::h_maxima(a, param, se_of(sen), o);
-      else if (op == "h_concave") geo::h_concave(a, param, se_of(sen), o);
-      else if (op == "h_convex") geo::h_convex(a, param, se_of(sen), o);
-      else if (op == "dynamic_pseudo_opening") geo::dynamic_pseudo_opening(a, param, se_of(sen), o);
-      else if (op == "dynamic_pseudo_closing") geo::dynamic_pseudo_closing(a, param, se_of(sen), o);
+      } else if (op == "h_minima") geo::h_minima(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
+      else if (op == "h_maxima") geo::h_maxima(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
+      else if (op == "h_concave") geo::h_concave(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
+      else if (op == "h_convex") geo::h_convex(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
+      else if (op == "dynamic_pseudo_opening") geo::dynamic_pseudo_opening(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
+      else if (op == "dynamic_pseudo_closing") geo::dynamic_pseudo_closing(a, PixelValue(a.GetDevicePType(), param), se_of(sen), o);
       else if (op == "label_binary") label::label_binary(a, se_of(sen), o);  // int64 in, int64 out
       else if (op == "label_flat_zones") label::label_flat_zones(a, se_of(sen), o);
       else if (op == "label_minima") label::label_minima(a, se_of(sen), o);
@@ -110,15 +110,18 @@ int main(int argc, char **argv) {
         std::vector<DeviceImage> ins;
         for (std::size_t k = 5; k < v.size(); ++k) ins.push_back(ImageFromString(v[k]));
         const auto tok = split(v[2], '|');
-        auto opnd = [&](const std::string &t) -> CompareOperand {
+        // a scalar holds the pixel type the reference's std::get<T> asks for: the input's for the
+        // comparand, the output's for the true / false values (compare.cpp:51-61)
+        auto opnd = [&](const std::string &t, PType pt) -> CompareOperand {
           if (t[0] == '#') return CompareOperand(std::stoi(t.substr(1)) == 0 ? (const IInterface &)a : ins.at(std::stoi(t.substr(1)) - 1));
-          return CompareOperand(std::stod(t));
+          return CompareOperand(PixelValue(pt, std::stod(t)));
         };
         static const std::map<std::string, CompOpType> ops = {
             {"equal", CompOpType::CompOpEqual}, {"diff", CompOpType::CompOpDiff}, {"sup", CompOpType::CompOpSup},
             {"sup_equal", CompOpType::CompOpSupEqual}, {"inf", CompOpType::CompOpInf},
             {"inf_equal", CompOpType::CompOpInfEqual}};
-        CompareImage(a, ops.at(sen), opnd(tok.at(0)), opnd(tok.at(1)), opnd(tok.at(2)), o);
+        const PType pi = a.GetDevicePType(), po = o.GetDevicePType();
+        CompareImage(a, ops.at(sen), opnd(tok.at(0), pi), opnd(tok.at(1), po), opnd(tok.at(2), po), o);
       }
       else { std::cerr << "unknown op " << op << "\n"; return 102; }
       ++run;
@@ -132,7 +135,8 @@ int main(int argc, char **argv) {
       std::cerr << "EXCEPTION " << op << " " << sen << ": " << e.what() << "\n";
     }
   }
-  // error behaviour: the reference throws std::runtime_error for these
+  // error behaviour: the reference throws std::runtime_error for these (for a scalar that does not
+  // hold the image's pixel type too: it rethrows std::get's bad_variant_access)
   int expected_throws = 0;
   try {
     DeviceImage a = ImageFromString("Scalar GUINT8 2 2 3 1 2 3 4 5 6");
@@ -148,7 +152,12 @@ int main(int argc, char **argv) {
     DeviceImage o = CloneGeometry(a);
     Dilate(a, se::Common_NL_SE::SESquare3D, 1, o);  // SE rank differs from the image's
   } catch (const std::runtime_error &) { ++expected_throws; }
-  if (expected_throws != 3) { std::cerr << "error behaviour differs\n"; ++failed; }
+  try {
+    DeviceImage a = ImageFromString("Scalar GUINT8 2 2 3 1 2 3 4 5 6");
+    DeviceImage o = CloneGeometry(a);
+    geo::h_maxima(a, ScalarTypeVariant(int32_t{1}), se::Common_NL_SE::SESquare2D, o);  // INT32 h, UINT8 image
+  } catch (const std::runtime_error &) { ++expected_throws; }
+  if (expected_throws != 4) { std::cerr << "error behaviour differs\n"; ++failed; }
   std::cout << "facade_test: " << run << " cases, " << failed << " failed\n";
   return failed;
 }

@@ -144,15 +144,23 @@ def test_pixel_processing_argument_checks_need_no_gpu(lib_path):
     assert L.pg_arith_invert_image(B(a), B(img(8, (8, 8), 0x10004)), None) == 5
     assert L.pg_convert_into(B(a), B(img(16, (8, 8), 0x10000)), None) == 5            # must be different
     assert L.pg_copy_into(B(a), B(wide), None) == 4
-    s = lambda v: _lib.PgOperand(None, v)  # noqa: E731
-    i = lambda d: _lib.PgOperand(ctypes.pointer(d), 0.0)  # noqa: E731
-    assert L.pg_compare_image(B(a), 3, B(s(1)), B(s(1)), B(s(0)), B(o), None) == 1     # not a CompOpType
-    assert L.pg_compare_image(B(a), 4, B(s(0.5)), B(s(1)), B(s(0)), B(o), None) == 1   # 0.5 is no INT32
-    assert L.pg_compare_image(B(a), 4, B(s(1)), B(s(300)), B(s(0)),
-                              B(img(4, (8, 8), 0x30000)), None) == 1                    # 300 is no UINT8
-    assert L.pg_compare_image(B(a), 4, B(i(img(32, (8, 8), 0x20000))), B(s(1)), B(s(0)), B(o), None) == 4
-    assert L.pg_compare_image(B(a), 4, B(s(1)), B(i(img(8, (8, 8), 0x20000))), B(s(0)), B(wide), None) == 4
-    assert L.pg_compare_image(B(a), 4, B(s(1)), B(s(1)), B(s(0)), B(img(8, (4, 16), 0x30000)), None) == 4
+    member = {4: "u8", 8: "i32", 16: "f32", 32: "i64"}
+
+    def s(pt, v):
+        sc = _lib.PgScalar()
+        sc.ptype = pt
+        setattr(sc.v, member[pt], v)
+        return _lib.PgOperand(None, sc)
+    i = lambda d: _lib.PgOperand(ctypes.pointer(d), _lib.PgScalar())  # noqa: E731
+    assert L.pg_compare_image(B(a), 3, B(s(8, 1)), B(s(8, 1)), B(s(8, 0)), B(o), None) == 1     # not a CompOpType
+    # a scalar that does not hold the pixel type std::get<T> asks for: PG_ERR_SCALAR_TYPE
+    assert L.pg_compare_image(B(a), 4, B(s(16, 0.5)), B(s(8, 1)), B(s(8, 0)), B(o), None) == 10  # FLOAT vs INT32 input
+    assert L.pg_compare_image(B(a), 4, B(s(8, 1)), B(s(8, 255)), B(s(4, 0)),
+                              B(img(4, (8, 8), 0x30000)), None) == 10                        # INT32 vs UINT8 output
+    assert b"unable to extract suitable type" in L.pg_last_error()
+    assert L.pg_compare_image(B(a), 4, B(i(img(32, (8, 8), 0x20000))), B(s(8, 1)), B(s(8, 0)), B(o), None) == 4
+    assert L.pg_compare_image(B(a), 4, B(s(8, 1)), B(i(img(8, (8, 8), 0x20000))), B(s(32, 0)), B(wide), None) == 4
+    assert L.pg_compare_image(B(a), 4, B(s(8, 1)), B(s(8, 1)), B(s(8, 0)), B(img(8, (4, 16), 0x30000)), None) == 4
 
 
 # pypoutre's function and enum names (python/*/*.cpp of poutre2), all present in the mirror
@@ -212,4 +220,25 @@ def test_square3d_reconstruction_is_refused_before_device_work(lib_path):
     m, k, o = img((4, 4, 4), 0x10000), img((4, 4, 4), 0x20000), img((4, 4, 4), 0x30000)
     B = ctypes.byref
     assert L.pg_reconstruction(1, B(m), B(k), 10, B(o), None) == 3
-    assert L.pg_h_maxima(B(m), 5.0, 10, B(o), None) == 3
+    h = _lib.scalar(4, 5)
+    assert L.pg_h_maxima(B(m), B(h), 10, B(o), None) == 3
+
+
+def test_exact_scalars_cross_the_boundary_without_rounding():
+    """pg_scalar carries every int64 value exactly (a double would round 2**62 + 1) and a Python value
+    that the pixel type cannot hold is refused like poutre2's std::get<T> refuses the variant."""
+    import numpy as np
+    from poutre2_gb300 import _lib
+    v = 2**62 + 1
+    assert _lib.scalar(32, v).v.i64 == v and _lib.scalar(32, v).ptype == 32
+    assert _lib.scalar(32, -2**63).v.i64 == -2**63
+    assert _lib.scalar(4, 20.0).v.u8 == 20
+    assert _lib.scalar(16, 0.1).v.f32 == np.float32(0.1)
+    assert _lib.scalar(8, np.float64(1.5)).ptype == 64  # a numpy scalar keeps its own type
+    for pt, bad in ((4, 256), (4, -1), (8, 0.5), (32, 2**63), (128, 70000), (16, "x"), (8, True)):
+        try:
+            _lib.scalar(pt, bad)
+        except _lib.PoutreError as e:
+            assert e.status == 10
+        else:
+            raise AssertionError((pt, bad))

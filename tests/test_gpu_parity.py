@@ -543,10 +543,12 @@ def test_errors_mirror_reference_checks():
         llm.Dilate(x, Common_NL_SE.SESquare2D, -1, torch.empty_like(x))
     with pytest.raises(PoutreError, match="NOT_SQUARE"):
         llm.DilateY(x, 2, torch.empty_like(x))
-    with pytest.raises(PoutreError, match="INVALID_ARGUMENT"):
+    with pytest.raises(PoutreError, match="SCALAR_TYPE"):
         geo.h_maxima(x, 3.5, Common_NL_SE.SESquare2D, torch.empty_like(x))
-    with pytest.raises(PoutreError, match="INVALID_ARGUMENT"):
+    with pytest.raises(PoutreError, match="SCALAR_TYPE"):
         geo.h_maxima(x, -1, Common_NL_SE.SESquare2D, torch.empty_like(x))
+    with pytest.raises(PoutreError, match="SCALAR_TYPE"):  # a numpy scalar keeps its type: INT32 for a UINT8 image
+        geo.h_maxima(x, np.int32(3), Common_NL_SE.SESquare2D, torch.empty_like(x))
     with pytest.raises(PoutreError, match="UNSUPPORTED_SE"):
         geo.Reconstruction(geo.reconstruction_type.dilate, x, x.clone(), Common_NL_SE.SESegmentX2D, torch.empty_like(x))
     with pytest.raises(PoutreError):
@@ -801,6 +803,22 @@ def test_copy_into_and_rejections():
         pixel.CompareImage(a, pixel.CompOpType.CompOpSup, a.to(torch.int64), 1, 0, o)
     with pytest.raises(PoutreError):  # a scalar that the pixel type cannot hold
         pixel.CompareImage(a, pixel.CompOpType.CompOpSup, 0.5, 1, 0, o)
+
+
+def test_int64_h_crosses_the_boundary_exactly():
+    """h = 2**53 + 1 on int64 pixels near 2**62: a double would round h to 2**53 and change the
+    h-maxima by one at every dome; the exact pg_scalar keeps it."""
+    from poutre2_gb300 import geo
+    from poutre2_gb300.se import Common_NL_SE
+    base = 2**62
+    f = smooth(5, (90, 120)).astype(np.int64) * (2**46) + base  # h = 128 grey levels + 1
+    h = 2**53 + 1
+    out = torch.empty_like(dev(f))
+    geo.h_maxima(dev(f), h, Common_NL_SE.SESquare2D, out)
+    exact = oracle.reconstruct(f - np.int64(h), f, "SESquare2D", True)
+    rounded = oracle.reconstruct(f - np.int64(float(h)), f, "SESquare2D", True)
+    assert not np.array_equal(exact, rounded)
+    np.testing.assert_array_equal(host(out), exact)
 
 
 def test_pypoutre_names():

@@ -54,11 +54,13 @@ def test_noalloc_matches_the_allocating_entry_point_on_consecutive_calls():
 
 
 def _shape_only(descriptor, dtype, shape):
-    """Descriptors of small real buffers whose shape fields claim `shape`: the entry point must
-    reject them on the host, from the shape alone, before any device work."""
+    """Descriptors whose shapes claim `shape`, at distinct addresses 2**40 bytes apart (so that no two
+    claimed buffers overlap): the entry point must reject them on the host, from the shape alone,
+    before any device work -- nothing is ever read or written through these pointers."""
     ds = []
-    for _ in range(3):
+    for k in range(3):
         d = descriptor(torch.zeros((4, 4), dtype=dtype, device="cuda"))
+        d.data = (k + 1) << 40
         d.rank = len(shape)
         for i, v in enumerate(shape):
             d.shape[i] = v
