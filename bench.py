@@ -270,7 +270,7 @@ def _time_ms(fn, flush, reps=5, warm=2):
 
 def extra_measurements(dev, flush, only=None):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
-    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048,
+    `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, large, cfg4, cfg5, label2048,
     pixel4096, octagon4096, geodesy3d), or
     all."""
     import numpy as np
@@ -343,11 +343,33 @@ def extra_measurements(dev, flush, only=None):
                     ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 5, 2)
                     rec(f"cfg3_{op}_{sname}_4096_{dt}", ms, x.numel(), 2 * x.numel() * es)
             del x, o
+        # the 3x3 square on a 4096^2 u8 image (the small-SE streaming kernel)
+        x8 = torch.from_numpy(synthetic.uniform_u8((4096, 4096), 2)).to(dev)
+        o8 = torch.empty_like(x8)
+        for dil in (True, False):
+            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(x8, Common_NL_SE.SESquare2D, 1, o8), flush, 10, 3)
+            rec(f"cfg3_{'dilate' if dil else 'erode'}_square3_4096_u8", ms, x8.numel(), 2 * x8.numel())
+        del x8, o8
         v = torch.from_numpy(synthetic.uniform_u8((256, 256, 256), 4)).to(dev)
         o = torch.empty_like(v)
         for dil in (True, False):
             ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(v, Common_NL_SE.SESquare3D, 1, o), flush, 10, 3)
             rec(f"cfg3_{'dilate' if dil else 'erode'}_cube3_256_u8", ms, v.numel(), 2 * v.numel())
+
+    def large():
+        # 16384^2 u16 (512 MiB in, 512 MiB out): the output is four times the 129 MB L2, so the
+        # timed kernel pays its own DRAM write-back and the fraction is a DRAM figure
+        rng = np.random.default_rng(2)
+        x = torch.from_numpy(rng.integers(0, 65536, (16384, 16384), dtype=np.uint16)).to(dev)
+        o = torch.empty_like(x)
+        for sname, se in (("square31", llm.se_rect(15, 15)), ("h63", llm.se_line(0, 1, 31)),
+                          ("v63", llm.se_line(1, 0, 31)), ("d45_63", llm.se_line(-1, 1, 31))):
+            for op, fn in (("dilate", llm.DilateSE), ("opening", llm.Opening)):
+                ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 3, 1)
+                rec(f"large_{op}_{sname}_16384_u16", ms, x.numel(), 4 * x.numel())
+        ms = _time_ms(lambda: llm.Dilate(x, Common_NL_SE.SESquare2D, 1, o), flush, 3, 1)
+        rec("large_dilate_square3_16384_u16", ms, x.numel(), 4 * x.numel())
+        del x, o
 
     def cfg4():
         imgs = synthetic.ragged_batch(512, 5, 4.0)
@@ -526,7 +548,7 @@ def extra_measurements(dev, flush, only=None):
                 pass
             rec(f"h_maxima_binary_{se}_128cube_u8", ms, f.size, 2 * f.size, **kw)
 
-    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, cfg4, cfg5, label2048, pixel4096, octagon4096, geodesy3d):
+    for fn in (cfg1, cfg2_4096, cfg2_leveling, cfg3, large, cfg4, cfg5, label2048, pixel4096, octagon4096, geodesy3d):
         if only is None or fn.__name__ in only:
             guard(fn)
     return res

@@ -355,6 +355,15 @@ PG_API pg_status pg_reconstruction_noalloc(int32_t type, const pg_image *marker,
  * observe the failure the reference would have thrown. */
 PG_API pg_status pg_check_device(pg_stream_t stream);
 
+/* Test hooks (no counterpart in the reference), for tests of the failure paths without a GPU fault.
+ * pg_debug_set_limits: max_rounds > 0 caps the reconstruction's rounds (round kernel) or visits per
+ * tile (worklist kernel), wait_ns > 0 sets the limit of every bounded device wait of the
+ * reconstruction kernels launched afterwards (default 4 s); a run that reaches either gives up and
+ * pg_check_device returns PG_ERR_NOT_CONVERGED.  0 restores the default.  Process-wide.
+ * pg_debug_fail_allocations: the next n temporary allocations fail (PG_ERR_OUT_OF_MEMORY). */
+PG_API pg_status pg_debug_set_limits(int32_t max_rounds, int64_t wait_ns);
+PG_API pg_status pg_debug_fail_allocations(int32_t n);
+
 /* Passes of the last completed reconstruction on the current device (diagnostics; synchronises
  * the device): for the shared-memory tile kernel the rounds of tile visits, for the worklist kernel
  * (pixels of at most 4 bytes) the tile visits divided by the number of tiles, rounded up. */

@@ -35,7 +35,7 @@ EXPORTED = [
     "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
     "pg_check_device", "pg_last_reconstruction_rounds", "pg_reconstruction_noalloc",
     "pg_h_maxima_binary_batch_plan", "pg_batch_plan_run", "pg_batch_plan_config", "pg_batch_plan_set_config",
-    "pg_batch_plan_destroy",
+    "pg_batch_plan_destroy", "pg_debug_set_limits", "pg_debug_fail_allocations",
 ]
 
 
@@ -171,6 +171,7 @@ def load(path: str | None = None):
             "pg_batch_plan_config": [VP, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)],
             "pg_batch_plan_set_config": [VP, I32, I32],
             "pg_batch_plan_destroy": [VP],
+            "pg_debug_set_limits": [I32, I64], "pg_debug_fail_allocations": [I32],
         }
         for name, args in sig.items():
             f = getattr(L, name)

@@ -10,11 +10,12 @@
 // when arg(p) == q -- no atomics, so the result is deterministic and equals a sequential
 // accumulation in raster order.
 //
-// GPU design: a CTA owns a 32x64 tile of one plane.  It stages x over the tile plus a 2r
-// halo, computes per row of the halo region the first-best value and column (separable
-// arg-extremum: the first row, in dy order, whose row-best is strictly best, then that
-// row's first column), stores the arg of every output that can reach the tile as one byte,
-// stages grad_out, and gathers.  Forward uses the same separable scheme without args.
+// GPU design: a CTA owns a tile of one plane.  It stages x over the tile plus a halo, computes per
+// row of the halo region the first-best value and column (separable arg-extremum: the first row, in
+// dy order, whose row-best is strictly best, then that row's first column), and for the backward
+// stages grad_out and gathers each input pixel's contributors.  Square windows of half size 1-3
+// have fixed-size kernels (k_flat_fwd_r, and k_flat_bwd_g for half sizes 1 and 2); other windows the
+// generic ones.
 #include <cmath>
 #include <atomic>
 
@@ -147,14 +148,9 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd(const float *__restrict
 }
 
 // ------------------------------------------------------------------ fixed window sizes
-// The same two kernels for a square (2R+1)^2 window known at compile time (R = 1, 2, 3): 2D thread
-// indexing (no integer division per element), unrolled window loops, staging loads issued before
-// the shared-memory stores, and a backward that does not test every window offset of every
-// output.  Backward: each routing output p sets bit `code` (its arg's position in its window) in
-// a 32-bit mask of the tile pixel q it routes to (shared atomicOr: order-free); then q adds the
-// upstream gradient of each contributor from the highest set bit to the lowest.  A higher code
-// means a contributor earlier in raster order, so the sum runs in the same order as the generic
-// kernel's gather and the result is bit-identical.  Needs (2R+1)^2 <= 32.
+// Kernels for a square (2R+1)^2 window known at compile time: 2D thread indexing (no integer
+// division per element), unrolled window loops, staging loads issued before the shared-memory
+// stores.
 static constexpr int AF_TX = 64, AF_TY = 4;  // 256 threads as 64 columns x 4 row groups
 
 template <bool SUP> __device__ __forceinline__ float best_of(float a, float b) { return SUP ? fmaxf(a, b) : fminf(a, b); }
@@ -219,31 +215,55 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_r(const float *__restri
   }
 }
 
+template <bool SUP>
+static bool flat_fwd_fixed(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int ry, int rx, cudaStream_t s) {
+  if (ry != rx || ry < 1 || ry > 3 || planes > 65535) return false;
+  const dim3 grid((unsigned)ceil_div(w, AF_TX - 2 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
+  if (ry == 1) k_flat_fwd_r<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
+  else if (ry == 2) k_flat_fwd_r<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
+  else k_flat_fwd_r<SUP, 3><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
+  return true;
+}
+
+// Backward for R = 1, 2 (the 3x3 and 5x5 squares), atomic-free.  With va(p) the window row of output
+// p's first-in-scan-order arg-extremum and ra(y, x) the column of the first-best pixel of row y's
+// window centred at x, output p routes to q iff  va(p) = 2R - a  for p = (q.y - R + a, .)  and
+// ra(q.y, p.x) = 2R - b  for p = (., q.x - R + b).  So:
+//   row pass    -- ra and the row-best value of every (x row, node column) of the tile's halo;
+//   column pass -- for every node (q row y, column x): the bits a of the outputs p = (y - R + a, x)
+//                  whose va is 2R - a (their row arg lands on row y), packed with ra(y, x) in one
+//                  word (bits a * (2R+1), ra at bit 28) -- a gather down the column, in registers;
+//   gather      -- q reads the words of nodes (q.y, q.x - R + b), keeps those whose ra points at q
+//                  (ra = 2R - b), shifts each by b, and so gets the mask of its contributors, bit
+//                  a * (2R+1) + b: raster order of the outputs.  It sums grad_out over the set bits
+//                  from the lowest, the order of a sequential accumulation in raster order of the
+//                  outputs, so the result is bit-identical to it.
+// No atomics.  Tile: AT_H x QW outputs, QW = 64 - 4R (the staged x band is one 64-thread row).
 template <bool SUP, int R>
-__global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restrict__ x, const float *__restrict__ gy,
+__global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restrict__ x, const float *__restrict__ gy,
                                                            float *__restrict__ gx, int H, int W) {
-  // Tile: AT_H x QW outputs, QW = 64 - 4R, so that the staged x band (QW + 4R) is exactly one
-  // column per thread of a 64-wide row and every phase is a single pass.
   constexpr int WX = 2 * R + 1;
-  static_assert(WX * WX <= 32, "codes must fit a 32-bit mask");
+  static_assert(WX * WX <= 28, "contributor mask and row arg must share one word");
+  constexpr unsigned MASK = (1u << (WX * WX)) - 1u;
   constexpr int QW = AF_TX - 4 * R;
-  constexpr int XH = AT_H + 4 * R, XW = AF_TX;         // x over the tile + 2R
-  constexpr int PH = AT_H + 2 * R, PW = QW + 2 * R;    // outputs that can route into the tile
-  constexpr int XR = (XH + AF_TY - 1) / AF_TY;         // staged x rows per thread
-  constexpr int PR = (PH + AF_TY - 1) / AF_TY;         // P rows per thread (contiguous)
+  constexpr int XH = AT_H + 4 * R, XW = AF_TX;       // x rows: tile rows -2R .. AT_H + 2R - 1
+  constexpr int PH = AT_H + 2 * R, PW = QW + 2 * R;  // outputs: tile rows / cols -R .. +R beyond the tile
+  constexpr int XR = (XH + AF_TY - 1) / AF_TY;       // staged x rows per thread
+  constexpr int GR = (PH + AF_TY - 1) / AF_TY;       // staged gradient rows per thread
+  constexpr int NR = AT_H / AF_TY;                   // node rows per thread (consecutive)
   __shared__ float X[XH][XW + 1];
   __shared__ float RV[XH][PW + 1];
   __shared__ unsigned char RA[XH][PW + 1];
   __shared__ float G[PH][PW + 1];
-  __shared__ unsigned M[AT_H][QW];
-  __shared__ unsigned short HEAVY[AT_H * QW];  // tile pixels left to the second gather pass
-  __shared__ int n_heavy;
+  __shared__ unsigned NODE[AT_H][PW + 1];
+  constexpr int WARP_PIX = AT_H / AF_TY * 32;                  // tile pixels a warp handles
+  __shared__ unsigned short HEAVY[AT_THREADS / 32][WARP_PIX];  // per warp: pixels left to the second pass
   const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
   const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * QW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *xp = x + plane;
   const float *gp = gy + plane;
-  {  // stage x and the upstream gradient, loads first; clear the masks
+  {  // stage x and the upstream gradient, loads first
     const int xx = tx0 - 2 * R + tx;
     const bool xin = xx >= 0 && xx < W;
     float v[XR];
@@ -254,9 +274,9 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restri
     }
     const int gxx = tx0 - R + tx;
     const bool gin = tx < PW && gxx >= 0 && gxx < W;
-    float g[PR];
+    float g[GR];
 #pragma unroll
-    for (int k = 0; k < PR; ++k) {
+    for (int k = 0; k < GR; ++k) {
       const int r = tq + k * AF_TY, yy = ty0 - R + r;
       g[k] = (r < PH && gin && yy >= 0 && yy < H) ? __ldg(gp + (int64_t)yy * W + gxx) : 0.f;
     }
@@ -266,18 +286,13 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restri
       if (r < XH) X[r][tx] = v[k];
     }
 #pragma unroll
-    for (int k = 0; k < PR; ++k) {
+    for (int k = 0; k < GR; ++k) {
       const int r = tq + k * AF_TY;
       if (r < PH && tx < PW) G[r][tx] = g[k];
     }
-    if (tx < QW) {
-#pragma unroll
-      for (int r = tq; r < AT_H; r += AF_TY) M[r][tx] = 0u;
-    }
-    if (threadIdx.x == 0) n_heavy = 0;
   }
   __syncthreads();
-  // row pass over the P columns: first strictly-best column of each row segment
+  // row pass over the node columns: first strictly-best column of each row segment
   if (tx < PW) {
 #pragma unroll
     for (int k = 0; k < XR; ++k) {
@@ -296,85 +311,91 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_r(const float *__restri
     }
   }
   __syncthreads();
-  // column pass: each routing output's arg code, posted as a bit to the tile pixel it routes to.
-  // Thread (tx, tq) walks P rows [tq * PR, tq * PR + PR) of column tx with the window in registers.
+  // column pass: thread (tx, tq) owns node rows [tq * NR, tq * NR + NR) of node column tx.  Node row
+  // y needs va of the outputs in P rows y .. y + 2R (output row y - R + a is P row y + a), and the
+  // output in P row pr takes its window rows from RV rows pr .. pr + 2R.
   if (tx < PW) {
     const int xx = tx0 - R + tx;
     const bool colin = xx >= 0 && xx < W;
-    const int r0 = tq * PR;
-    float col[PR + 2 * R];
+    const int y0 = tq * NR;
+    float col[NR + 4 * R];
 #pragma unroll
-    for (int i = 0; i < PR + 2 * R; ++i) col[i] = (r0 + i < XH) ? RV[r0 + i][tx] : outside<SUP>();
+    for (int i = 0; i < NR + 4 * R; ++i) col[i] = RV[y0 + i][tx];
+    unsigned va[NR + 2 * R];  // 0xff for outputs outside the image: never a route
 #pragma unroll
-    for (int i = 0; i < PR; ++i) {
-      const int r = r0 + i, yy = ty0 - R + r;
-      if (r >= PH || !colin || yy < 0 || yy >= H) continue;  // not an output
+    for (int i = 0; i < NR + 2 * R; ++i) {
       float b = col[i];
-      int a = 0;
+      unsigned a = 0;
 #pragma unroll
       for (int d = 1; d <= 2 * R; ++d)
         if (better<SUP>(col[i + d], b)) { b = col[i + d]; a = d; }
-      const int ac = RA[r + a][tx];
-      // the arg in tile coordinates: output (r - R, tx - R) + window (a - R, ac - R)
-      const int qr = r - 2 * R + a, qc = tx - 2 * R + ac;
-      if (qr >= 0 && qr < AT_H && qc >= 0 && qc < QW) atomicOr(&M[qr][qc], 1u << (a * WX + ac));
+      const int oy = ty0 - R + y0 + i;  // image row of the output in P row y0 + i
+      va[i] = (colin && oy >= 0 && oy < H) ? a : 0xffu;
+    }
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      unsigned vm = 0u;
+#pragma unroll
+      for (int a = 0; a <= 2 * R; ++a) vm |= (va[j + a] == (unsigned)(2 * R - a) ? 1u : 0u) << (a * WX);
+      NODE[y0 + j][tx] = vm | ((unsigned)RA[y0 + j + 2 * R][tx] << 28);
     }
   }
   __syncthreads();
-  // gather: contributors in raster order = codes from high to low.  Code c's contributor sits at
-  // G[r + 2R - c / WX][tx + 2R - c % WX].  A pixel with more than two contributors (a local
-  // extremum collects up to WX^2) goes to a list handled in a second pass, so that one lane's
-  // long chain does not hold up its warp.
-  auto gather = [&](int r, int c) -> float {
-    unsigned m = M[r][c];
-    const float *gq = &G[r + 2 * R][c + 2 * R];
+  // gather in raster order of the contributors; a pixel with more than two of them (a local extremum
+  // collects up to (2R+1)^2) goes to a list handled in a second pass, so that one lane's long chain
+  // does not hold up its warp
+  auto mask_of = [&](int r, int c) -> unsigned {
+    unsigned m = 0u;
+#pragma unroll
+    for (int b = 0; b <= 2 * R; ++b) {
+      const unsigned w = NODE[r][c + b];
+      if ((w >> 28) == (unsigned)(2 * R - b)) m |= (w & MASK) << b;
+    }
+    return m;
+  };
+  auto gather = [&](int r, int c, unsigned m) -> float {
     float sum = 0.f;
     while (m) {
-      const int code = 31 - __clz(m);
-      m ^= 1u << code;
-      const int a = code / WX;
-      sum += gq[-(a * (PW + 1) + (code - a * WX))];
+      const int bit = __ffs(m) - 1;
+      m &= m - 1u;
+      const int a = bit / WX, b = bit - a * WX;
+      sum += G[r + a][c + b];
     }
     return sum;
   };
+  // (each warp keeps its own list, filled by ballot: no shared counter)
   float *op = gx + plane;
-  if (tx < QW) {
+  const int lane = threadIdx.x & 31;
+  unsigned short *heavy = HEAVY[threadIdx.x / 32];
+  int n_heavy = 0;  // warp-uniform
+  {
     const int xx = tx0 + tx;
 #pragma unroll 4
     for (int r = tq; r < AT_H; r += AF_TY) {
       const int yy = ty0 + r;
-      if (yy >= H || xx >= W) continue;
-      if (__popc(M[r][tx]) > 2) {
-        HEAVY[atomicAdd(&n_heavy, 1)] = (unsigned short)(r * QW + tx);
-        continue;
-      }
-      op[(int64_t)yy * W + xx] = gather(r, tx);
+      const bool mine = tx < QW && yy < H && xx < W;
+      const unsigned m = mine ? mask_of(r, tx) : 0u;
+      const bool defer = __popc(m) > 2;
+      const unsigned db = __ballot_sync(0xffffffffu, defer);
+      if (defer) heavy[n_heavy + __popc(db & ((1u << lane) - 1u))] = (unsigned short)(r * QW + tx);
+      else if (mine) op[(int64_t)yy * W + xx] = gather(r, tx, m);
+      n_heavy += __popc(db);
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n_heavy; i += AT_THREADS) {
-    const int q = HEAVY[i], r = q / QW, c = q - r * QW;
-    op[(int64_t)(ty0 + r) * W + tx0 + c] = gather(r, c);
+  __syncwarp();
+  for (int i = lane; i < n_heavy; i += 32) {
+    const int q = heavy[i], r = q / QW, c = q - r * QW;
+    op[(int64_t)(ty0 + r) * W + tx0 + c] = gather(r, c, mask_of(r, c));
   }
-}
-
-template <bool SUP>
-static bool flat_fwd_fixed(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int ry, int rx, cudaStream_t s) {
-  if (ry != rx || ry < 1 || ry > 3 || planes > 65535) return false;
-  const dim3 grid((unsigned)ceil_div(w, AF_TX - 2 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
-  if (ry == 1) k_flat_fwd_r<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
-  else if (ry == 2) k_flat_fwd_r<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
-  else k_flat_fwd_r<SUP, 3><<<grid, AT_THREADS, 0, s>>>(x, y, (int)h, (int)w);
-  return true;
 }
 
 template <bool SUP>
 static bool flat_bwd_fixed(const float *x, const float *g, float *o, int64_t planes, int64_t h, int64_t w, int ry, int rx,
                            cudaStream_t s) {
-  if (ry != rx || ry < 1 || ry > 2 || planes > 65535) return false;  // (2R+1)^2 <= 32
+  if (ry != rx || ry < 1 || ry > 2 || planes > 65535) return false;
   const dim3 grid((unsigned)ceil_div(w, AF_TX - 4 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
-  if (ry == 1) k_flat_bwd_r<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
-  else k_flat_bwd_r<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
+  if (ry == 1) k_flat_bwd_g<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
+  else k_flat_bwd_g<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
   return true;
 }
 

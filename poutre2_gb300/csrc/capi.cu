@@ -2,6 +2,7 @@
 // (AssertSizesCompatible / AssertAsTypesCompatible / AssertImagesAreDifferent, the
 // rank x PType x SE switches of src/low_level_morpho/*.cpp and src/geodesy/*.cpp), then
 // dispatch to the kernels.  No exception crosses the boundary.
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -24,6 +25,15 @@ pg_status cuda_status(cudaError_t e, const char *what) {
   if (e == cudaSuccess) return PG_OK;
   t_err = std::string(what) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? PG_ERR_OUT_OF_MEMORY : PG_ERR_CUDA;
+}
+
+static std::atomic<int> g_alloc_failures{0};
+
+bool take_injected_alloc_failure() {
+  int n = g_alloc_failures.load();
+  while (n > 0)
+    if (g_alloc_failures.compare_exchange_weak(n, n - 1)) return true;
+  return false;
 }
 
 void retain_pool_memory() {
@@ -386,6 +396,13 @@ extern "C" {
 
 const char *pg_last_error(void) { return t_err.c_str(); }
 const char *pg_version(void) { return "poutre2_gb300 0.1 (sm_103a)"; }
+
+// Test hook: the next n temporary allocations fail as if the device were out of memory.
+pg_status pg_debug_fail_allocations(int32_t n) {
+  if (n < 0) return pg::fail(PG_ERR_INVALID_ARGUMENT, "pg_debug_fail_allocations: negative count");
+  pg::g_alloc_failures.store(n);
+  return PG_OK;
+}
 
 // ---------------------------------------------------------------- low_level_morpho
 pg_status pg_erode(const pg_image *in, int32_t se, int32_t iter, const pg_image *out, pg_stream_t s) {

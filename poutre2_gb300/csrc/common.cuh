@@ -152,6 +152,9 @@ pg_status recon_se(int se, int rank, bool &conn8);
 // fresh pages again; the pool keeps up to kPoolRetainBytes instead (set once per device).
 static constexpr uint64_t kPoolRetainBytes = 1ull << 30;
 void retain_pool_memory();
+// Test hook (pg_debug_fail_allocations): true while injected allocation failures remain; each call
+// that returns true uses one up.
+bool take_injected_alloc_failure();
 
 struct Scratch {
   void *ptr = nullptr;
@@ -162,6 +165,8 @@ struct Scratch {
   pg_status alloc(size_t bytes, cudaStream_t s) {
     retain_pool_memory();
     stream = s;
+    if (take_injected_alloc_failure())
+      return fail(PG_ERR_OUT_OF_MEMORY, "temporary allocation of " + std::to_string(bytes) + " bytes failed (injected)");
     cudaError_t e = cudaMallocAsync(&ptr, bytes ? bytes : 16, s);
     if (e != cudaSuccess) {
       ptr = nullptr;

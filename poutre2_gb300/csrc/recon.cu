@@ -47,6 +47,12 @@ template <typename T> __host__ __device__ constexpr int tile_side() { return til
 static constexpr int kMaxSweeps = 512;
 static constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;  // 4 s
 
+// Limits that a test may lower (pg_debug_set_limits): the device wait limit, passed to every launch
+// and used by every bounded wait below, and a cap on the rounds (round kernel) / visits per tile
+// (worklist kernel) that replaces the host's default when positive.
+static std::atomic<unsigned long long> g_dbg_wait_ns{kBarrierTimeoutNs};
+static std::atomic<int> g_dbg_max_rounds{0};
+
 // Device-wide sticky status of the reconstruction kernels (0 = ok) and the round count of
 // the last completed launch.
 __device__ int g_recon_status = 0;
@@ -81,6 +87,7 @@ template <typename T> struct RParams {
   unsigned *flags;    // 2 * ntiles
   int max_rounds;
   int max_sweeps = kMaxSweeps;  // sweep sets per tile visit before the tile yields (and re-flags itself)
+  unsigned long long wait_ns = kBarrierTimeoutNs;  // limit of every bounded device wait
   int init, mask_mode, epi;
   T h;
 };
@@ -103,6 +110,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+
 __device__ __forceinline__ void set_status(RCtl *ctl, int code) {
   atomicCAS(&ctl->status, 0, code);
   atomicCAS(&g_recon_status, 0, code);
@@ -110,7 +118,7 @@ __device__ __forceinline__ void set_status(RCtl *ctl, int code) {
 
 // Grid barrier with a bounded wait.  Returns false once any CTA recorded an error; thread 0
 // reads the status for its whole CTA so that every thread takes the same branch afterwards.
-__device__ bool grid_barrier(RCtl *ctl) {
+__device__ bool grid_barrier(RCtl *ctl, unsigned long long wait_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -128,7 +136,7 @@ __device__ bool grid_barrier(RCtl *ctl) {
       while (*genp == gen) {
         __nanosleep(ns);
         if (ns < 1024) ns <<= 1;
-        if (global_ns() - t0 > kBarrierTimeoutNs) {
+        if (global_ns() - t0 > wait_ns) {
           set_status(ctl, PG_ERR_NOT_CONVERGED);
           break;
         }
@@ -492,7 +500,7 @@ __global__ void __launch_bounds__(RT) k_reconstruct(RParams<T> P) {
         process_tile<T, SUP, CONN8, RT>(im, P, tl, round, s_out, s_mask, &s_flag);
       }
     }
-    if (!grid_barrier(ctl)) { ok = false; break; }
+    if (!grid_barrier(ctl, P.wait_ns)) { ok = false; break; }
     const unsigned any = *((volatile unsigned *)&ctl->any[(round + 1) % 3]);
     ++round;
     if (!any) break;
@@ -968,10 +976,11 @@ template <typename T> struct WorkList {
   unsigned *state;             // ntiles
   unsigned long long *ring;    // cap slots
   unsigned cap;
+  unsigned long long wait_ns;  // limit of every bounded wait
 };
 
-__device__ __forceinline__ bool wait_expired(RCtl *ctl, unsigned long long t0) {
-  if (global_ns() - t0 > kBarrierTimeoutNs) {
+__device__ __forceinline__ bool wait_expired(RCtl *ctl, unsigned long long t0, unsigned long long wait_ns) {
+  if (global_ns() - t0 > wait_ns) {
     set_status(ctl, PG_ERR_NOT_CONVERGED);
     return true;
   }
@@ -1001,7 +1010,7 @@ __device__ int wl_pop(const WorkList<T> &wl, RCtl *ctl, long long max_tickets) {
     if (*((volatile int *)&ctl->status) != 0) return -1;
     __nanosleep(ns);
     if (ns < 4096) ns <<= 1;
-    if (wait_expired(ctl, t0)) return -1;
+    if (wait_expired(ctl, t0, wl.wait_ns)) return -1;
   }
   *slot = slot_val(pos, 0u);  // consumed: the next lap's pusher may write
   const unsigned tile = (unsigned)v - 1u;
@@ -1072,7 +1081,7 @@ __device__ void wl_finish(const WorkList<T> &wl, RCtl *ctl, const RImg &im, int 
     const unsigned long long t0 = global_ns();
     while (*slot != want) {
       __nanosleep(64);
-      if (wait_expired(ctl, t0)) break;
+      if (wait_expired(ctl, t0, wl.wait_ns)) break;
     }
     *slot = slot_val(pos, (unsigned)cand + 1u);
   }
@@ -1132,7 +1141,7 @@ __global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T>
   if (tid == 0) {
     wl.q->tp = ((unsigned long long)P.ntiles << 32) | (unsigned long long)P.ntiles;
   }
-  if (!grid_barrier(ctl)) return;
+  if (!grid_barrier(ctl, P.wait_ns)) return;
 
   // phase 1: visits until no tile is queued or running
   // runaway guard on the tickets (visits plus idle pops), also below the wrap of the 32-bit ring
@@ -1151,7 +1160,7 @@ __global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T>
     wl_finish<T, CONN8>(wl, ctl, im, t, tl, f);
     __syncwarp();
   }
-  if (!grid_barrier(ctl)) return;
+  if (!grid_barrier(ctl, P.wait_ns)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const long long visits = (long long)tp_tail(*((volatile unsigned long long *)&wl.q->tp));  // every pushed tile was visited
     g_recon_visits = visits;
@@ -1167,6 +1176,15 @@ __global__ void __launch_bounds__(kRegWarps * 32, 4) k_reconstruct_wl(RParams<T>
 // words: the double-buffered flags of the round kernel, or the tile states and the ring of the
 // worklist.  The work area is cleared before the launch.
 static constexpr size_t kWorkHead = 256 + sizeof(RQueue);
+
+// Rounds (round kernel) or visits per tile (worklist kernel) before a launch gives up: far more than
+// any input needs (a tile is revisited only when a neighbour changed its border), unless a test set
+// a cap through pg_debug_set_limits.
+static int max_rounds_for(int64_t ntiles) {
+  const int cap = g_dbg_max_rounds.load();
+  if (cap > 0) return cap;
+  return (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * ntiles);
+}
 static unsigned ring_cap(int64_t ntiles) { return (unsigned)(2 * ntiles + 4096); }
 static size_t ring_offset(int64_t ntiles) { return ((4 * (size_t)ntiles + 255) / 256) * 256; }
 static size_t work_bytes(int64_t ntiles) {
@@ -1183,8 +1201,10 @@ static pg_status launch_recon(RParams<T> &P, char *work, cudaStream_t s, int *gr
   constexpr int TILES_PER_CTA = REG ? kRegWarps : 1;
   P.ctl = reinterpret_cast<RCtl *>(work);
   P.flags = reinterpret_cast<unsigned *>(work + kWorkHead);
-  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * (int64_t)P.ntiles);
+  P.max_rounds = max_rounds_for(P.ntiles);
+  P.wait_ns = g_dbg_wait_ns.load();
   WorkList<T> wl{};
+  wl.wait_ns = P.wait_ns;
   wl.q = reinterpret_cast<RQueue *>(work + 256);
   wl.state = P.flags;
   wl.ring = reinterpret_cast<unsigned long long *>(work + kWorkHead + ring_offset(P.ntiles));
@@ -1564,7 +1584,8 @@ static pg_status run_noalloc_t(RImg im, cudaStream_t s) {
   P.ntiles = (int)ntiles;
   P.ctl = static_cast<RCtl *>(base);
   P.flags = reinterpret_cast<unsigned *>(static_cast<char *>(base) + kNoAllocFlagsOffset);
-  P.max_rounds = (int)std::min<int64_t>(INT32_MAX / 2, 1024 + 64 * ntiles);
+  P.max_rounds = max_rounds_for(ntiles);
+  P.wait_ns = g_dbg_wait_ns.load();
   P.init = INIT_MARKER;
   P.mask_mode = MASK_PLAIN;
   P.epi = EPI_NONE;
@@ -1626,6 +1647,15 @@ pg_status pg_check_device(pg_stream_t stream) {
     return pg::fail(static_cast<pg_status>(os), "an opening tile load did not complete within its wait limit");
   if (const int ls = pg::take_label_status())
     return pg::fail(static_cast<pg_status>(ls), "a labelling union-find loop exceeded its iteration limit");
+  return PG_OK;
+}
+
+// Test hooks: lower the reconstruction's round / visit cap and its device wait limit so that a test
+// can make a bounded wait run out and read PG_ERR_NOT_CONVERGED back; 0 restores the defaults.
+pg_status pg_debug_set_limits(int32_t max_rounds, int64_t wait_ns) {
+  if (max_rounds < 0 || wait_ns < 0) return pg::fail(PG_ERR_INVALID_ARGUMENT, "pg_debug_set_limits: negative limit");
+  pg::g_dbg_max_rounds.store(max_rounds);
+  pg::g_dbg_wait_ns.store(wait_ns > 0 ? (unsigned long long)wait_ns : pg::kBarrierTimeoutNs);
   return PG_OK;
 }
 

@@ -9,18 +9,27 @@
 // what runs here (for SESquare3D poutre2 stops short of it, and that SE is refused):
 //   prep     -- the initial value (marker clamped to the mask, or the mask shifted by h) and, for
 //               leveling, the effective mask max(marker, ref) / min(marker, ref);
-//   step     -- one voxel per thread: the extremum over the SE's voxels inside the volume, clamped to
-//               the mask, into the other buffer; a warp vote sets a change flag;
+//   brick    -- a CTA loads a brick of 32 x 8 x 8 voxels of the current value (plus a one-voxel halo)
+//               and of the mask into shared memory and repeats the geodesic step on the brick, the
+//               halo held fixed, until the brick stops changing (or an iteration cap); it writes the
+//               brick to the other buffer and sets a change flag when any voxel differs from its
+//               input.  Every update is a geodesic step from a lower bound of the fixpoint (monotone
+//               and below it), so the order is immaterial; a launch that changes nothing is the
+//               fixpoint.  One launch carries values across a whole brick, where a plain step moves
+//               them one voxel;
 //   epilogue -- the reconstruction itself, its clip to the leveling reference, or the binary
 //               h-maxima output ref > rec.
-// The host runs the steps in batches of kStepBatch between two reads of the flag; a step that
-// changes nothing is a fixpoint, and after at most (voxels + 1) steps one always is.
+// The host runs the launches in batches of kStepBatch between two reads of the flag; a launch that
+// changes nothing is a fixpoint, and after at most (voxels + 1) launches one always is (each launch
+// does at least one geodesic step everywhere).
 #include "common.cuh"
 
 namespace pg {
 namespace {
 
-constexpr int kStepBatch = 8;
+constexpr int kStepBatch = 2;
+constexpr int kBX = 32, kBY = 8, kBZ = 8;  // brick
+constexpr int kBrickIters = 2 * (kBX + kBY + kBZ);  // local iteration cap per launch
 
 template <typename T, bool SUP> __device__ __forceinline__ T shift_h(T m, T h) {
   return SUP ? sat_sub_c(m, h) : sat_add_c(m, h);  // h-maxima marker f - h, h-minima marker f + h
@@ -45,25 +54,67 @@ __global__ void k_r3_prep(const T *__restrict__ ref, const T *__restrict__ marke
 }
 
 template <typename T, bool SUP>
-__global__ void __launch_bounds__(256) k_r3_step(const T *__restrict__ cur, const T *__restrict__ mask,
-                                                 T *__restrict__ next, int D, int H, int W, int *__restrict__ changed) {
-  const int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  const int y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
-  const int z = (int)blockIdx.z;
+__global__ void __launch_bounds__(kBX * kBY) k_r3_brick(const T *__restrict__ cur, const T *__restrict__ mask,
+                                                        T *__restrict__ next, int D, int H, int W,
+                                                        int *__restrict__ changed) {
+  constexpr int HX = kBX + 2, HY = kBY + 2, HZ = kBZ + 2;
+  __shared__ T sr[HZ][HY][HX];      // current value with a one-voxel halo
+  __shared__ T sk[kBZ][kBY][kBX];   // mask of the brick
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kBX + tx;
+  const int x0 = blockIdx.x * kBX, y0 = blockIdx.y * kBY, z0 = blockIdx.z * kBZ;
+  const int64_t plane = (int64_t)H * W;
+  const T NEU = Op<T, SUP>::neutral();  // never wins the extremum: voxels outside the volume
+  for (int i = tid; i < HX * HY * HZ; i += kBX * kBY) {
+    const int hx = i % HX, hy = (i / HX) % HY, hz = i / (HX * HY);
+    const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+    sr[hz][hy][hx] = (x >= 0 && x < W && y >= 0 && y < H && z >= 0 && z < D) ? cur[z * plane + (int64_t)y * W + x] : NEU;
+  }
+  const int x = x0 + tx, y = y0 + ty;
+  const bool xy_in = x < W && y < H;
+#pragma unroll
+  for (int k = 0; k < kBZ; ++k) {
+    const int z = z0 + k;
+    sk[k][ty][tx] = (xy_in && z < D) ? mask[z * plane + (int64_t)y * W + x] : NEU;
+  }
+  __syncthreads();
+  T start[kBZ];
+#pragma unroll
+  for (int k = 0; k < kBZ; ++k) start[k] = sr[k + 1][ty + 1][tx + 1];
+  // this thread's z column, updated in place (values only move towards the fixpoint, so reading a
+  // neighbour's old or new value are both valid steps)
+  for (int it = 0; it < kBrickIters; ++it) {
+    bool ch = false;
+    if (xy_in) {
+#pragma unroll
+      for (int k = 0; k < kBZ; ++k) {
+        if (z0 + k >= D) break;
+        volatile T *c = &sr[k + 1][ty + 1][tx + 1];
+        const T v = *c;
+        T n = Op<T, SUP>::apply(v, sr[k + 1][ty + 1][tx]);
+        n = Op<T, SUP>::apply(n, sr[k + 1][ty + 1][tx + 2]);
+        n = Op<T, SUP>::apply(n, sr[k + 1][ty][tx + 1]);
+        n = Op<T, SUP>::apply(n, sr[k + 1][ty + 2][tx + 1]);
+        n = Op<T, SUP>::apply(n, sr[k][ty + 1][tx + 1]);
+        n = Op<T, SUP>::apply(n, sr[k + 2][ty + 1][tx + 1]);
+        n = Op<T, !SUP>::apply(n, sk[k][ty][tx]);
+        if (!(n == v)) {
+          *c = n;
+          ch = true;
+        }
+      }
+    }
+    if (!__syncthreads_or(ch)) break;
+  }
   bool diff = false;
-  if (x < W && y < H) {
-    const int64_t c = ((int64_t)z * H + y) * W + x;
-    const T v0 = cur[c];
-    T v = v0;  // the SECross3D voxels inside the volume
-    if (x > 0) v = Op<T, SUP>::apply(v, cur[c - 1]);
-    if (x + 1 < W) v = Op<T, SUP>::apply(v, cur[c + 1]);
-    if (y > 0) v = Op<T, SUP>::apply(v, cur[c - W]);
-    if (y + 1 < H) v = Op<T, SUP>::apply(v, cur[c + W]);
-    if (z > 0) v = Op<T, SUP>::apply(v, cur[c - (int64_t)H * W]);
-    if (z + 1 < D) v = Op<T, SUP>::apply(v, cur[c + (int64_t)H * W]);
-    v = Op<T, !SUP>::apply(v, mask[c]);
-    next[c] = v;
-    diff = !(v == v0);
+  if (xy_in) {
+#pragma unroll
+    for (int k = 0; k < kBZ; ++k) {
+      const int z = z0 + k;
+      if (z >= D) break;
+      const T v = sr[k + 1][ty + 1][tx + 1];
+      next[z * plane + (int64_t)y * W + x] = v;
+      diff |= !(v == start[k]);
+    }
   }
   if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(changed, 1);
 }
@@ -91,7 +142,8 @@ pg_status recon3d_t(const pg_image *marker, const pg_image &mask, const pg_image
   const Dims d = dims_of(mask);
   const int64_t n = d.count();
   if (n == 0) return PG_OK;
-  if (d.nz > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "3D reconstruction: more than 65535 slices");
+  if (d.nx > INT32_MAX || d.ny > INT32_MAX || d.nz > INT32_MAX || ceil_div(d.ny, kBY) > 65535 || ceil_div(d.nz, kBZ) > 65535)
+    return fail(PG_ERR_INVALID_ARGUMENT, "3D reconstruction: volume too large (ny <= 524280, nz <= 524280)");
   if (rq.init != INIT_SAT_CONST && !marker) return fail(PG_ERR_INVALID_ARGUMENT, "3D reconstruction: null marker");
   const size_t bytes = (size_t)n * sizeof(T);
   const bool own_mask = rq.init != INIT_SAT_CONST && rq.mask_mode != MASK_PLAIN;
@@ -107,18 +159,18 @@ pg_status recon3d_t(const pg_image *marker, const pg_image &mask, const pg_image
                                                  own_mask ? static_cast<T *>(emask.ptr) : nullptr, a, n, rq.init,
                                                  rq.mask_mode, scalar_as<T>(rq.h));
   PG_CUDA_TRY(cudaGetLastError(), "3D reconstruction prep launch");
-  const dim3 block(32, 8), grid((unsigned)ceil_div(d.nx, 32), (unsigned)ceil_div(d.ny, 8), (unsigned)d.nz);
+  const dim3 block(kBX, kBY), grid((unsigned)ceil_div(d.nx, kBX), (unsigned)ceil_div(d.ny, kBY), (unsigned)ceil_div(d.nz, kBZ));
   const int64_t max_steps = n + kStepBatch + 1;
   int64_t steps = 0;
   for (;;) {
     PG_CUDA_TRY(cudaMemsetAsync(d_flag, 0, sizeof(int), s), "3D reconstruction flag reset");
     for (int k = 0; k < kStepBatch; ++k) {
-      k_r3_step<T, SUP><<<grid, block, 0, s>>>(a, eff, b, (int)d.nz, (int)d.ny, (int)d.nx, d_flag);
+      k_r3_brick<T, SUP><<<grid, block, 0, s>>>(a, eff, b, (int)d.nz, (int)d.ny, (int)d.nx, d_flag);
       T *t = a;
       a = b;
       b = t;
     }
-    PG_CUDA_TRY(cudaGetLastError(), "3D reconstruction step launch");
+    PG_CUDA_TRY(cudaGetLastError(), "3D reconstruction brick launch");
     steps += kStepBatch;
     int h_flag = 0;
     PG_CUDA_TRY(cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s), "3D reconstruction flag read");

@@ -86,13 +86,14 @@ def test_noalloc_size_limit_of_its_fixed_scratch():
 def test_noalloc_refuses_volumes_and_keeps_the_reference_checks():
     L, descriptor, stream = _setup()
     v = torch.zeros((4, 5, 6), dtype=torch.uint8, device="cuda")
-    m, k, o = descriptor(v), descriptor(v.clone()), descriptor(torch.empty_like(v))
+    vk, vo = v.clone(), torch.empty_like(v)  # held: a descriptor keeps only the address
+    m, k, o = descriptor(v), descriptor(vk), descriptor(vo)
     assert L.pg_reconstruction_noalloc(1, ctypes.byref(m), ctypes.byref(k), 9, ctypes.byref(o), stream) == 3
     assert b"1D and 2D" in L.pg_last_error()
     x = torch.zeros((8, 8), dtype=torch.uint8, device="cuda")
-    dx, dy = descriptor(x), descriptor(x.clone())
+    y, z = x.clone(), torch.empty_like(x)
+    dx, dy, dz = descriptor(x), descriptor(y), descriptor(z)
     # output aliasing the mask: PG_ERR_ALIASING, as pg_reconstruction
     assert L.pg_reconstruction_noalloc(1, ctypes.byref(dy), ctypes.byref(dx), 2, ctypes.byref(dx), stream) == 5
     # a 3D SE on an image: PG_ERR_UNSUPPORTED_SE, as pg_reconstruction
-    assert L.pg_reconstruction_noalloc(1, ctypes.byref(dy), ctypes.byref(dx), 9,
-                                       ctypes.byref(descriptor(torch.empty_like(x))), stream) == 3
+    assert L.pg_reconstruction_noalloc(1, ctypes.byref(dy), ctypes.byref(dx), 9, ctypes.byref(dz), stream) == 3
