@@ -268,7 +268,7 @@ def _time_ms(fn, flush, reps=5, warm=2):
     return statistics.median(out)
 
 
-def extra_measurements(dev, flush, only=None):
+def extra_measurements(dev, flush, only=None, cfg5_batch=64):
     """The other workloads (parity-tested in tests/test_gpu_fullsize.py), timed the same way.
     `only`: names of the groups to run (cfg1, cfg2_4096, cfg2_leveling, cfg3, large, cfg4, cfg5, label2048,
     pixel4096, octagon4096, geodesy3d), or
@@ -418,7 +418,7 @@ def extra_measurements(dev, flush, only=None):
         plan.close()
 
     def cfg5():
-        shape = (64, 32, 256, 256)
+        shape = (cfg5_batch, 32, 256, 256)  # the workload's batch is 64; a smaller one only for profiling
         x = torch.randn(shape, device=dev, generator=torch.Generator(device=dev).manual_seed(6))
         g = torch.randn(shape, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
         n = x.numel()
@@ -432,8 +432,9 @@ def extra_measurements(dev, flush, only=None):
                 fn(xr, 2).backward(g)
             fb_ms = _time_ms(fb, flush, 3, 1)
             passes = 2 if name == "opening" else 1
-            rec(f"cfg5_{name}_5x5_fwd_64x32x256x256_f32", fwd, n, passes * 2 * n * 4)
-            rec(f"cfg5_{name}_5x5_fwd_bwd_64x32x256x256_f32", fb_ms, n, passes * 5 * n * 4, fwd_bwd_over_fwd=fb_ms / fwd)
+            tag = f"{cfg5_batch}x32x256x256"
+            rec(f"cfg5_{name}_5x5_fwd_{tag}_f32", fwd, n, passes * 2 * n * 4)
+            rec(f"cfg5_{name}_5x5_fwd_bwd_{tag}_f32", fb_ms, n, passes * 5 * n * 4, fwd_bwd_over_fwd=fb_ms / fwd)
             del xr
 
     def label2048():
@@ -672,7 +673,7 @@ def run_gpu(args):
                                              f"loops, auto-vectorised by the compiler)"}
         if args.extra:
             only = set(args.only.split(",")) if args.only else None
-            line["extra"] = extra_measurements(dev, flush, only)
+            line["extra"] = extra_measurements(dev, flush, only, args.cfg5_batch)
         print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()
@@ -691,6 +692,8 @@ def main():
     ap.add_argument("--no-extra", dest="extra", action="store_false")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--only", default="", help="comma-separated subset of the extra workloads (e.g. cfg3,cfg5)")
+    ap.add_argument("--cfg5-batch", type=int, default=64, help="first dimension of the cfg5 tensor (64 = the workload; "
+                                                              "smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -239,27 +239,44 @@ static bool flat_fwd_fixed(const float *x, float *y, int64_t planes, int64_t h, 
 //                  from the lowest, the order of a sequential accumulation in raster order of the
 //                  outputs, so the result is bit-identical to it.
 // No atomics.  Tile: AT_H x QW outputs, QW = 64 - 4R (the staged x band is one 64-thread row).
-template <bool SUP, int R>
+// Shared-memory layout of k_flat_bwd_g for a tile of TH rows (bytes, each part 16-byte aligned).  The
+// node words reuse the staged x once the row pass has read it.
+template <int R, int TH> struct BwdG {
+  static constexpr int WX = 2 * R + 1, QW = AF_TX - 4 * R, XH = TH + 4 * R, XW = AF_TX + 1;
+  static constexpr int PH = TH + 2 * R, PW = QW + 2 * R + 1;  // padded pitches (+1)
+  static constexpr int WARP_PIX = TH / AF_TY * 32;           // tile pixels a warp handles
+  static constexpr size_t al(size_t b) { return (b + 15) / 16 * 16; }
+  static constexpr size_t X_OFF = 0, X_BYTES = al((size_t)XH * XW * 4);  // x, later the node words
+  static constexpr size_t RV_OFF = X_OFF + X_BYTES, RV_BYTES = al((size_t)XH * PW * 4);
+  static constexpr size_t G_OFF = RV_OFF + RV_BYTES, G_BYTES = al((size_t)PH * PW * 4);
+  static constexpr size_t RA_OFF = G_OFF + G_BYTES, RA_BYTES = al((size_t)XH * PW);
+  static constexpr size_t H_OFF = RA_OFF + RA_BYTES, H_BYTES = al((size_t)(AT_THREADS / 32) * WARP_PIX * 2);
+  static constexpr size_t smem = H_OFF + H_BYTES;
+  static_assert((size_t)TH * PW * 4 <= X_BYTES, "node words must fit in the x buffer");
+};
+
+template <bool SUP, int R, int TH>
 __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restrict__ x, const float *__restrict__ gy,
                                                            float *__restrict__ gx, int H, int W) {
-  constexpr int WX = 2 * R + 1;
+  using L = BwdG<R, TH>;
+  constexpr int WX = L::WX;
   static_assert(WX * WX <= 28, "contributor mask and row arg must share one word");
   constexpr unsigned MASK = (1u << (WX * WX)) - 1u;
-  constexpr int QW = AF_TX - 4 * R;
-  constexpr int XH = AT_H + 4 * R, XW = AF_TX;       // x rows: tile rows -2R .. AT_H + 2R - 1
-  constexpr int PH = AT_H + 2 * R, PW = QW + 2 * R;  // outputs: tile rows / cols -R .. +R beyond the tile
+  constexpr int QW = L::QW;
+  constexpr int XH = L::XH, XW = L::XW;               // x rows: tile rows -2R .. TH + 2R - 1
+  constexpr int PH = L::PH, PW = QW + 2 * R, PP = L::PW;  // outputs: tile rows / cols -R .. +R beyond the tile
   constexpr int XR = (XH + AF_TY - 1) / AF_TY;       // staged x rows per thread
   constexpr int GR = (PH + AF_TY - 1) / AF_TY;       // staged gradient rows per thread
-  constexpr int NR = AT_H / AF_TY;                   // node rows per thread (consecutive)
-  __shared__ float X[XH][XW + 1];
-  __shared__ float RV[XH][PW + 1];
-  __shared__ unsigned char RA[XH][PW + 1];
-  __shared__ float G[PH][PW + 1];
-  __shared__ unsigned NODE[AT_H][PW + 1];
-  constexpr int WARP_PIX = AT_H / AF_TY * 32;                  // tile pixels a warp handles
-  __shared__ unsigned short HEAVY[AT_THREADS / 32][WARP_PIX];  // per warp: pixels left to the second pass
+  constexpr int NR = TH / AF_TY;                     // node rows per thread (consecutive)
+  extern __shared__ __align__(16) unsigned char smb[];
+  float(*X)[XW] = reinterpret_cast<float(*)[XW]>(smb + L::X_OFF);
+  unsigned(*NODE)[PP] = reinterpret_cast<unsigned(*)[PP]>(smb + L::X_OFF);  // after the row pass
+  float(*RV)[PP] = reinterpret_cast<float(*)[PP]>(smb + L::RV_OFF);
+  float(*G)[PP] = reinterpret_cast<float(*)[PP]>(smb + L::G_OFF);
+  unsigned char(*RA)[PP] = reinterpret_cast<unsigned char(*)[PP]>(smb + L::RA_OFF);
+  unsigned short *HEAVY = reinterpret_cast<unsigned short *>(smb + L::H_OFF);
   const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
-  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * QW;
+  const int ty0 = blockIdx.y * TH, tx0 = blockIdx.x * QW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *xp = x + plane;
   const float *gp = gy + plane;
@@ -310,10 +327,12 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restri
       }
     }
   }
-  __syncthreads();
+  __syncthreads();  // x is dead from here on: its buffer takes the node words
   // column pass: thread (tx, tq) owns node rows [tq * NR, tq * NR + NR) of node column tx.  Node row
   // y needs va of the outputs in P rows y .. y + 2R (output row y - R + a is P row y + a), and the
-  // output in P row pr takes its window rows from RV rows pr .. pr + 2R.
+  // output in P row pr takes its window rows from RV rows pr .. pr + 2R.  The node's word holds those
+  // bits already shifted by its own b = 2R - ra (its column offset seen from the pixel it routes to),
+  // with that b at bit 28.
   if (tx < PW) {
     const int xx = tx0 - R + tx;
     const bool colin = xx >= 0 && xx < W;
@@ -337,19 +356,20 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restri
       unsigned vm = 0u;
 #pragma unroll
       for (int a = 0; a <= 2 * R; ++a) vm |= (va[j + a] == (unsigned)(2 * R - a) ? 1u : 0u) << (a * WX);
-      NODE[y0 + j][tx] = vm | ((unsigned)RA[y0 + j + 2 * R][tx] << 28);
+      const unsigned bsh = (unsigned)(2 * R) - RA[y0 + j + 2 * R][tx];
+      NODE[y0 + j][tx] = (vm << bsh) | (bsh << 28);
     }
   }
   __syncthreads();
   // gather in raster order of the contributors; a pixel with more than two of them (a local extremum
-  // collects up to (2R+1)^2) goes to a list handled in a second pass, so that one lane's long chain
-  // does not hold up its warp
+  // collects up to (2R+1)^2) goes to its warp's list, handled in a second pass, so that one lane's long
+  // chain does not hold up its warp (each warp keeps its own list, filled by ballot: no shared counter)
   auto mask_of = [&](int r, int c) -> unsigned {
     unsigned m = 0u;
 #pragma unroll
     for (int b = 0; b <= 2 * R; ++b) {
       const unsigned w = NODE[r][c + b];
-      if ((w >> 28) == (unsigned)(2 * R - b)) m |= (w & MASK) << b;
+      if ((w >> 28) == (unsigned)b) m |= w & MASK;
     }
     return m;
   };
@@ -363,15 +383,14 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restri
     }
     return sum;
   };
-  // (each warp keeps its own list, filled by ballot: no shared counter)
   float *op = gx + plane;
   const int lane = threadIdx.x & 31;
-  unsigned short *heavy = HEAVY[threadIdx.x / 32];
+  unsigned short *heavy = HEAVY + (threadIdx.x / 32) * L::WARP_PIX;
   int n_heavy = 0;  // warp-uniform
   {
     const int xx = tx0 + tx;
 #pragma unroll 4
-    for (int r = tq; r < AT_H; r += AF_TY) {
+    for (int r = tq; r < TH; r += AF_TY) {
       const int yy = ty0 + r;
       const bool mine = tx < QW && yy < H && xx < W;
       const unsigned m = mine ? mask_of(r, tx) : 0u;
@@ -389,13 +408,32 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_g(const float *__restri
   }
 }
 
+template <bool SUP, int R, int TH>
+static pg_status bwd_g_launch(const float *x, const float *g, float *o, int64_t planes, int64_t h, int64_t w,
+                              cudaStream_t s) {
+  using L = BwdG<R, TH>;
+  static std::atomic<uint64_t> attr{0};
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(attr.load() & bit)) {
+    PG_CUDA_TRY(cudaFuncSetAttribute(k_flat_bwd_g<SUP, R, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::smem),
+                "backward smem attribute");
+    attr.fetch_or(bit);
+  }
+  const dim3 grid((unsigned)ceil_div(w, L::QW), (unsigned)ceil_div(h, TH), (unsigned)planes);
+  k_flat_bwd_g<SUP, R, TH><<<grid, AT_THREADS, L::smem, s>>>(x, g, o, (int)h, (int)w);
+  return cuda_status(cudaGetLastError(), "flat morphology backward launch");
+}
+
+// rows per backward tile: taller tiles stage less halo per pixel, at more shared memory per CTA
+static constexpr int kBwdTileH = 32;
+
 template <bool SUP>
 static bool flat_bwd_fixed(const float *x, const float *g, float *o, int64_t planes, int64_t h, int64_t w, int ry, int rx,
-                           cudaStream_t s) {
-  if (ry != rx || ry < 1 || ry > 2 || planes > 65535) return false;
-  const dim3 grid((unsigned)ceil_div(w, AF_TX - 4 * ry), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
-  if (ry == 1) k_flat_bwd_g<SUP, 1><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
-  else k_flat_bwd_g<SUP, 2><<<grid, AT_THREADS, 0, s>>>(x, g, o, (int)h, (int)w);
+                           cudaStream_t s, pg_status *st) {
+  if (ry != rx || ry < 1 || ry > 2 || planes > 65535 || ceil_div(h, kBwdTileH) > 65535) return false;
+  *st = ry == 1 ? bwd_g_launch<SUP, 1, kBwdTileH>(x, g, o, planes, h, w, s) : bwd_g_launch<SUP, 2, kBwdTileH>(x, g, o, planes, h, w, s);
   return true;
 }
 
@@ -449,9 +487,10 @@ pg_status launch_flat2d_backward(const float *x, const float *gy, float *gx, int
   if (ry < 0 || rx < 0 || ry > AR_MAX || rx > AR_MAX) return fail(PG_ERR_INVALID_ARGUMENT, "half sizes must be in [0, 7]");
   if (planes * h * w == 0) return PG_OK;
   if (h > (1 << 30) || w > (1 << 30) || ceil_div(h, AT_H) > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "plane too large");
-  if (dilate ? flat_bwd_fixed<true>(x, gy, gx, planes, h, w, ry, rx, s)
-             : flat_bwd_fixed<false>(x, gy, gx, planes, h, w, ry, rx, s))
-    return cuda_status(cudaGetLastError(), "flat morphology backward launch");
+  pg_status st = PG_OK;
+  if (dilate ? flat_bwd_fixed<true>(x, gy, gx, planes, h, w, ry, rx, s, &st)
+             : flat_bwd_fixed<false>(x, gy, gx, planes, h, w, ry, rx, s, &st))
+    return st;
   static std::atomic<uint64_t> fs{0}, fe{0};
   const size_t sm = bwd_smem(ry, rx);
   if (dilate) {
