@@ -234,7 +234,7 @@ PG_API pg_status pg_h_maxima_binary_batch(const pg_image *ins, const pg_image *o
  * tables, the worklist and the reconstruction buffers stay on the device, so a run is one
  * memset plus one persistent cooperative launch, both of which can be captured in a CUDA graph.
  * With autotune != 0 the plan times tile side (32: register tiles, a warp per tile; 64: shared-
- * memory tiles, a 64-thread CTA per tile) x sweep sets per tile visit (4, 16, unbounded) on this
+ * memory tiles, a 64-thread CTA per tile) x sweep sets per tile visit (2, 4, 16, unbounded) on this
  * batch and keeps the fastest; the choice is cached per (pixel type, connectivity, batch size
  * class).  Without autotune the configuration is 32 / unbounded.  Images of rank 1 or 2.  Inputs/outputs must stay valid
  * while the plan is used.  Plan creation synchronises the device.
