@@ -541,7 +541,7 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
         o = torch.empty_like(x)
         for se in ("SECross3D",):
             ms = _time_ms(lambda se=se: geo.h_maxima_binary(x, 10, Common_NL_SE[se], o, check=False), flush, 5, 2)
-            kw = {"note": "includes the host reads of the change flag (every 8 steps)"}
+            kw = {"note": "includes the host reads of the change flag (every two brick launches)"}
             try:
                 from oracle import ref
                 if ref.available():
