@@ -257,10 +257,15 @@ bool try_line_stream(const pg_image &in, const pg_image &out, int dy, int dx, in
                      pg_status *st);
 bool try_line_words(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
                     pg_status *st);
-// 45- / 135-degree segments of 2k+1 pixels through TMA parallelogram tiles (diag.cu): k = 7, 15, 31;
-// u16, i32 and f32 images with rows of a multiple of 16 bytes.
-bool try_diag_tile(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
-                   pg_status *st);
+// Vertical, 45- and 135-degree segments (dy = 1, dx = 0 / -1 / +1) of 2k+1 pixels through TMA
+// parallelogram tiles (diag.cu): k = 7 (not u8), 15, 31; u8, u16, i32 and f32 images with rows of a
+// multiple of 16 bytes.  try_segment_open: the opening (closing) by that segment in one pass.
+bool try_segment_tile(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool dilate, cudaStream_t s,
+                      pg_status *st);
+bool try_segment_open(const pg_image &in, const pg_image &out, int dy, int dx, int k, bool opening, cudaStream_t s,
+                      pg_status *st);
+bool try_segment_gradient(const pg_image &in, const pg_image &out, int dy, int dx, int k, cudaStream_t s,
+                          pg_status *st);  // dilation - erosion by that segment in one pass
 int take_diag_status();  // device status of the diagonal tile kernel since the last call (0: none)
 pg_status launch_rect(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s);
 // One-pass box (rect.cu): (hy, hx) = (k, k), (0, k) or (k, 0), k in {7, 15, 31}; 2-/4-byte pixels,

@@ -194,7 +194,7 @@ pg_status launch_line(const pg_image &in, const pg_image &out, int dy, int dx, i
   const int64_t k = std::min<int64_t>(half, std::max<int64_t>(kmax, 0));
   if (k >= 1 && k <= (1 << 20)) {
     pg_status st = PG_OK;
-    if (try_diag_tile(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
+    if (dx != 0 && try_segment_tile(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
     if (try_line_stream(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
     if (try_line_words(in, out, dy, dx, (int)k, dilate, s, &st)) return st;
   }
