@@ -245,10 +245,13 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- GPU arm
 def _time_ms(fn, flush, reps=5, warm=2):
-    """Median CUDA-event time of fn() on the current stream, L2 flushed before each rep.  A GPU-side
-    wait of about 100 us is queued after the flush, so that fn's launches are already enqueued when
-    the stream reaches the first event: the bracket times the device work, not the host's launch
-    path (which for a 10-20 us kernel is of the same order)."""
+    """CUDA-event time of fn() on the current stream, L2 flushed before each rep.  A GPU-side wait of
+    about 100 us is queued after the flush, so that fn's launches are already enqueued when the stream
+    reaches the first event: the bracket times the device work, not the host's launch path (which for
+    a 10-20 us kernel is of the same order).  The GB300's event clock advances in 2.048 us steps, so a
+    single reading of a 15 us kernel is off by up to 14 %; with at least 12 reps the mean of the middle
+    readings (a fifth dropped at each end) is returned, which averages the steps out -- fewer reps, the
+    median."""
     import torch
     for _ in range(warm):
         fn()
@@ -265,6 +268,10 @@ def _time_ms(fn, flush, reps=5, warm=2):
         b.record(st)
         torch.cuda.synchronize()
         out.append(a.elapsed_time(b))
+    if len(out) >= 12:
+        out.sort()
+        cut = len(out) // 5
+        return statistics.fmean(out[cut:len(out) - cut])
     return statistics.median(out)
 
 
@@ -344,20 +351,20 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
                               ("v63", llm.se_line(1, 0, 31)), ("d45_63", llm.se_line(-1, 1, 31))):
                 for op, fn in (("dilate", llm.DilateSE), ("erode", llm.ErodeSE), ("opening", llm.Opening),
                                ("closing", llm.Closing), ("gradient", llm.Gradient)):
-                    ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 5, 2)
+                    ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 15, 2)
                     rec(f"cfg3_{op}_{sname}_4096_{dt}", ms, x.numel(), 2 * x.numel() * es)
             del x, o
         # the 3x3 square on a 4096^2 u8 image (the small-SE streaming kernel)
         x8 = torch.from_numpy(synthetic.uniform_u8((4096, 4096), 2)).to(dev)
         o8 = torch.empty_like(x8)
         for dil in (True, False):
-            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(x8, Common_NL_SE.SESquare2D, 1, o8), flush, 10, 3)
+            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(x8, Common_NL_SE.SESquare2D, 1, o8), flush, 15, 3)
             rec(f"cfg3_{'dilate' if dil else 'erode'}_square3_4096_u8", ms, x8.numel(), 2 * x8.numel())
         del x8, o8
         v = torch.from_numpy(synthetic.uniform_u8((256, 256, 256), 4)).to(dev)
         o = torch.empty_like(v)
         for dil in (True, False):
-            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(v, Common_NL_SE.SESquare3D, 1, o), flush, 10, 3)
+            ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(v, Common_NL_SE.SESquare3D, 1, o), flush, 15, 3)
             rec(f"cfg3_{'dilate' if dil else 'erode'}_cube3_256_u8", ms, v.numel(), 2 * v.numel())
 
     def large():
@@ -368,7 +375,7 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
         o = torch.empty_like(x)
         for sname, se in (("square31", llm.se_rect(15, 15)), ("h63", llm.se_line(0, 1, 31)),
                           ("v63", llm.se_line(1, 0, 31)), ("d45_63", llm.se_line(-1, 1, 31))):
-            for op, fn in (("dilate", llm.DilateSE), ("opening", llm.Opening)):
+            for op, fn in (("dilate", llm.DilateSE), ("opening", llm.Opening), ("gradient", llm.Gradient)):
                 ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 3, 1)
                 rec(f"large_{op}_{sname}_16384_u16", ms, x.numel(), 4 * x.numel())
         ms = _time_ms(lambda: llm.Dilate(x, Common_NL_SE.SESquare2D, 1, o), flush, 3, 1)
@@ -517,7 +524,7 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
             x = torch.from_numpy(a).to(dev)
             o = torch.empty_like(x)
             for size in (5, 10):
-                ms = _time_ms(lambda: llm.Dilate(x, Compound_NL_SE.Octagon, size, o), flush, 10, 3)
+                ms = _time_ms(lambda: llm.Dilate(x, Compound_NL_SE.Octagon, size, o), flush, 15, 3)
                 kw = {}
                 try:
                     from oracle import ref

@@ -71,7 +71,9 @@ template <typename T, int K, int DIR, bool FUSED> struct DiagGeom {
   static constexpr int NV = NT / TW;                     // thread groups stacked along the tile's rows
   static constexpr int CH = W2 / G * G;                  // windows per van Herk chunk
   static constexpr int KH = FUSED ? 2 * K : K;           // input rows above the first output row
-  static constexpr int BWP = TW + (DIR != 0 ? G : 0);    // box width, pixels
+  // box width, pixels: a whole number of 16-byte chunks with G rows of it a multiple of 128 bytes, so
+  // that the groups lie back to back in shared memory (the 45-degree tile arrives as one 3D box)
+  static constexpr int BWP = ceil_to(TW + (DIR != 0 ? G : 0), 8);
   static constexpr int RP = BWP * S;                     // bytes per box row
   static constexpr int GP = ceil_to(G * RP, 128);        // bytes per group in shared memory (TMA: 128-aligned)
   static constexpr int THG = FUSED ? fused_rows(G, CH, K, GP) : (120 / NV) / CH * CH;  // output rows per group
@@ -88,6 +90,7 @@ template <typename T, int K, int DIR, bool FUSED> struct DiagGeom {
   static constexpr size_t smem = (size_t)(BR / G) * GP + 16;  // + the mbarrier
   static_assert(CH >= G && THG >= CH && NT % TW == 0 && BWP <= 256 && TH % G == 0 && BR % RB == 0,
                 "segment tile geometry");
+  static_assert(GP == G * RP, "groups back to back in shared memory");
   static_assert(!FUSED || NC2 * CH + 2 * K <= NC1 * CH + 2 * K, "second scan inside the first scan's rows");
   static_assert(FUSED || THG % CH == 0, "single scan: whole chunks");
 };
@@ -164,7 +167,8 @@ template <typename T> __device__ __forceinline__ T grad_of(T d, T e) {
 // MODE: 0 erosion, 1 dilation, 2 opening (erosion, then dilation), 3 closing, 4 gradient (dilation - erosion)
 template <typename T, int K, int DIR, int MODE>
 __global__ void __launch_bounds__(DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>::NT, (MODE == 4 ? 3 : 0))
-    k_segment_tile(const __grid_constant__ CUtensorMap tmap, T *__restrict__ out, int H, int W) {
+    k_segment_tile(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap smap,
+                   T *__restrict__ out, int H, int W, int shear_rows) {
   constexpr bool FUSED = MODE == 2 || MODE == 3;
   constexpr bool GRAD = MODE == 4;
   using Gm = DiagGeom<T, K, DIR, FUSED>;
@@ -199,7 +203,18 @@ __global__ void __launch_bounds__(DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>:
   }
   __syncthreads();
   if (!s_ok) return;
-  if (tid < 32) {
+  // 45 degrees: the whole staircase is one box of the sheared view `smap` (group j of the view starts
+  // 16 bytes left of row G*j, so view column X of group j is image column X - G*j), unless the tile
+  // reaches the last H mod G rows, which the view leaves out (shear_rows = G * floor(H / G))
+  const bool sheared = DIR > 0 && shear_rows > 0 && (shear_rows == H || ty + BR <= shear_rows);
+  if (sheared) {
+    if (tid == 0)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+              smem_u32(s_box)),
+          "l"(&smap), "r"(box_x(0) + ty), "r"(0), "r"(ty / G), "r"(bar_a)
+          : "memory");
+  } else if (tid < 32) {
     for (int b = tid; b < NB; b += 32) {
       const int g = b * (RB / G);
       asm volatile(
@@ -220,11 +235,15 @@ __global__ void __launch_bounds__(DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>:
   if (!s_ok) return;
   (void)mbar_try(bar_a, 0);  // the phase is complete: each thread observes it (acquire)
 
-  // pixels outside the image: TMA wrote zeros; the first operator needs its neutral value there
-  if constexpr (!GRAD && !(std::is_unsigned_v<T> && SUP_A)) {
+  // pixels outside the image: the 2D boxes hold TMA's zero fill there, the sheared view zeros above and
+  // below the image but, left and right of it, pixels of the neighbouring rows; the first operator
+  // needs its neutral value at all of them (zero already is it for the dilation of unsigned pixels,
+  // unless the sheared view brought neighbouring rows in)
+  if constexpr (!GRAD) {
     const int xa = box_x(0), xb = box_x(BR / G - 1);
     const int xlo = DIR > 0 ? xb : xa, xhi = (DIR > 0 ? xa : xb) + BWP;
-    if (ty < 0 || ty + BR > H || xlo < 0 || xhi > W) {
+    constexpr bool zero_neutral = std::is_unsigned_v<T> && SUP_A;
+    if ((!zero_neutral && (ty < 0 || ty + BR > H || xlo < 0 || xhi > W)) || (zero_neutral && sheared && (xlo < 0 || xhi > W))) {
       const T NEU = OA::neutral();
       for (int r = tid; r < BR; r += Gm::NT) {
         const int g = r / G;
@@ -376,13 +395,39 @@ pg_status pixel_map(CUtensorMap *map, const void *data, int64_t H, int64_t W, in
   return PG_OK;
 }
 
+// Sheared view of the same image for 45-degree tiles: dims (X, k, j) -> image row G*j + k, column
+// X - G*j, with j < floor(H / G) and X < W + G*(floor(H / G) - 1).  Every coordinate inside those
+// bounds addresses a pixel of the image buffer: the largest is row G*floor(H/G) - 1 <= H - 1 at a
+// column <= W - 1, the smallest the first pixel, so the view reads nothing outside the buffer; left and
+// right of the image it reads pixels of the neighbouring rows, which the kernel then overwrites.  Box:
+// bw pixels x G rows x groups.  False if the driver refuses the view (the kernel then uses 2D boxes).
+bool sheared_map(CUtensorMap *map, const void *data, int64_t H, int64_t W, int S, int bw, int G, int groups) {
+  auto fn = encode_tiled();
+  if (!fn) return false;
+  const int64_t Jn = H / G;
+  cuuint64_t dims[3] = {(cuuint64_t)(W + G * (Jn - 1)), (cuuint64_t)G, (cuuint64_t)Jn};
+  cuuint64_t strides[2] = {(cuuint64_t)W * S, (cuuint64_t)(G * W * S - 16)};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)G, (cuuint32_t)groups};
+  cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = S == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                 : S == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                                          : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  return fn(map, dt, 3, const_cast<void *>(data), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
 template <typename T, int K, int DIR, int MODE>
 pg_status segment_tile(const pg_image &in, const pg_image &out, cudaStream_t s) {
   using Gm = DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>;
   const Dims d = dims_of(in);
   const int64_t H = d.ny, W = d.nx;
-  CUtensorMap map;
+  CUtensorMap map, smap;
   PG_TRY(pixel_map(&map, in.data, H, W, Gm::S, Gm::BWP, Gm::RB));
+  int shear_rows = 0;
+  smap = map;
+  if (DIR > 0 && H >= Gm::G && sheared_map(&smap, in.data, H, W, Gm::S, Gm::BWP, Gm::G, Gm::BR / Gm::G))
+    shear_rows = (int)(H / Gm::G * Gm::G);
   static std::atomic<uint64_t> attr_devices{0};
   int dev = 0;
   PG_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
@@ -396,7 +441,8 @@ pg_status segment_tile(const pg_image &in, const pg_image &out, cudaStream_t s) 
   const int64_t gy = ceil_div(H + Gm::D, Gm::TH);
   if (gy > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the segment tile kernel");
   const dim3 grid((unsigned)DiagCols<Gm, DIR>::count(W), (unsigned)gy);
-  k_segment_tile<T, K, DIR, MODE><<<grid, Gm::NT, Gm::smem, s>>>(map, static_cast<T *>(out.data), (int)H, (int)W);
+  k_segment_tile<T, K, DIR, MODE><<<grid, Gm::NT, Gm::smem, s>>>(map, smap, static_cast<T *>(out.data), (int)H, (int)W,
+                                                                  shear_rows);
   return cuda_status(cudaGetLastError(), "segment tile launch");
 }
 
