@@ -233,6 +233,10 @@ static pg_status compound(const pg_image &in, int compound_se, int size, const p
   const double nb = (double)size / (1.0 + std::sqrt(2.0));
   const double fl = std::floor(nb);
   const int nb_square = (int)((nb - fl) < 0.5 ? fl : fl + 1);
+  if (in.rank == 2) {  // all passes in one shared-memory tile kernel (octagon.cu)
+    pg_status st = PG_OK;
+    if (try_octagon_tile(in, out, size - nb_square, nb_square, dilate, s, &st)) return st;
+  }
   std::vector<int> passes;
   passes.push_back(cross);
   for (int i = 1; i < size - nb_square; ++i) passes.push_back(cross);

@@ -1654,7 +1654,9 @@ pg_status pg_check_device(pg_stream_t stream) {
   if (const int rs = pg::take_rect_status())
     return pg::fail(static_cast<pg_status>(rs), "a box tile load did not complete within its wait limit");
   if (const int ds = pg::take_diag_status())
-    return pg::fail(static_cast<pg_status>(ds), "a diagonal tile load did not complete within its wait limit");
+    return pg::fail(static_cast<pg_status>(ds), "a segment tile load did not complete within its wait limit");
+  if (const int os8 = pg::take_oct_status())
+    return pg::fail(static_cast<pg_status>(os8), "an octagon tile load did not complete within its wait limit");
   if (const int os = pg::take_open_status())
     return pg::fail(static_cast<pg_status>(os), "an opening tile load did not complete within its wait limit");
   if (const int ls = pg::take_label_status())
