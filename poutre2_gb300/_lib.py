@@ -32,7 +32,8 @@ EXPORTED = [
     "pg_sat_sub_constant", "pg_sat_add_constant",
     "pg_arith_invert_image", "pg_arith_sup_image", "pg_arith_inf_image", "pg_sat_add_image", "pg_sat_sub_image",
     "pg_compare_image", "pg_copy_into", "pg_convert_into",
-    "pg_flat_morph2d_forward", "pg_flat_morph2d_backward",
+    "pg_flat_morph2d_forward", "pg_flat_morph2d_backward", "pg_flat_morph2d_forward_arg",
+    "pg_flat_morph2d_backward_arg",
     "pg_check_device", "pg_last_reconstruction_rounds", "pg_reconstruction_noalloc",
     "pg_h_maxima_binary_batch_plan", "pg_batch_plan_run", "pg_batch_plan_config", "pg_batch_plan_set_config",
     "pg_batch_plan_destroy", "pg_debug_set_limits", "pg_debug_fail_allocations",
@@ -164,6 +165,8 @@ def load(path: str | None = None):
             "pg_copy_into": [img, img, VP], "pg_convert_into": [img, img, VP],
             "pg_flat_morph2d_forward": [fp, fp, I64, I64, I64, I32, I32, I32, VP],
             "pg_flat_morph2d_backward": [fp, fp, fp, I64, I64, I64, I32, I32, I32, VP],
+            "pg_flat_morph2d_forward_arg": [fp, fp, VP, I64, I64, I64, I32, I32, VP],
+            "pg_flat_morph2d_backward_arg": [VP, fp, fp, I64, I64, I64, I32, VP],
             "pg_check_device": [VP],
             "pg_reconstruction_noalloc": [I32, img, img, I32, img, VP],
             "pg_h_maxima_binary_batch_plan": [img, img, I32, D, I32, I32, ctypes.POINTER(VP), VP],

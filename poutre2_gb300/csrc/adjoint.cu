@@ -215,6 +215,158 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_r(const float *__restri
   }
 }
 
+// Forward that also saves each output's arg code for the backward: code(p) = a * (2R+1) + b, (a, b)
+// the window row and column of p's first-in-scan-order arg-extremum (the first strictly-best row of
+// the window, then that row's first strictly-best column, as k_flat_bwd computes them; 255 is never
+// written for an image pixel).  The values are the same best_of chains as k_flat_fwd_r, so y is
+// bit-identical to the plain forward.
+template <bool SUP, int R>
+__global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__restrict__ x, float *__restrict__ y,
+                                                             unsigned char *__restrict__ code, int H, int W) {
+  constexpr int FW = AF_TX - 2 * R, WX = 2 * R + 1;
+  constexpr int XH = AT_H + 2 * R, XW = AF_TX;
+  __shared__ float X[XH][XW + 1];
+  __shared__ float RV[XH][FW + 1];   // row-best values (best_of chain)
+  __shared__ float RB[XH][FW + 1];   // row-best values of the strict-better chain (equal to RV without NaN)
+  __shared__ unsigned char RA[XH][FW + 1];
+  const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
+  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * FW;
+  const int64_t plane = (int64_t)blockIdx.z * H * W;
+  const float *xp = x + plane;
+  constexpr int RI = (XH + AF_TY - 1) / AF_TY;
+  {
+    const int gx = tx0 - R + tx;
+    const bool colin = gx >= 0 && gx < W;
+    float v[RI];
+#pragma unroll
+    for (int k = 0; k < RI; ++k) {
+      const int r = tq + k * AF_TY, gy = ty0 - R + r;
+      v[k] = (r < XH && colin && gy >= 0 && gy < H) ? __ldg(xp + (int64_t)gy * W + gx) : outside<SUP>();
+    }
+#pragma unroll
+    for (int k = 0; k < RI; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < XH) X[r][tx] = v[k];
+    }
+  }
+  __syncthreads();
+  if (tx < FW) {
+#pragma unroll
+    for (int k = 0; k < RI; ++k) {
+      const int r = tq + k * AF_TY;
+      if (r < XH) {
+        float b = X[r][tx], bb = b;
+        int a = 0;
+#pragma unroll
+        for (int d = 1; d <= 2 * R; ++d) {
+          const float v = X[r][tx + d];
+          b = best_of<SUP>(b, v);
+          if (better<SUP>(v, bb)) { bb = v; a = d; }
+        }
+        RV[r][tx] = b;
+        RB[r][tx] = bb;
+        RA[r][tx] = (unsigned char)a;
+      }
+    }
+  }
+  __syncthreads();
+  if (tx < FW) {
+    float *yp = y + plane;
+    unsigned char *cp = code + plane;
+    constexpr int OR = AT_H / AF_TY;
+    const int r0 = tq * OR, gx = tx0 + tx;
+    float col[OR + 2 * R], colb[OR + 2 * R];
+#pragma unroll
+    for (int i = 0; i < OR + 2 * R; ++i) {
+      col[i] = RV[r0 + i][tx];
+      colb[i] = RB[r0 + i][tx];
+    }
+#pragma unroll
+    for (int i = 0; i < OR; ++i) {
+      float b = col[i], bb = colb[i];
+      int a = 0;
+#pragma unroll
+      for (int d = 1; d <= 2 * R; ++d) {
+        b = best_of<SUP>(b, col[i + d]);
+        if (better<SUP>(colb[i + d], bb)) { bb = colb[i + d]; a = d; }
+      }
+      const int gy = ty0 + r0 + i;
+      if (gy < H && gx < W) {
+        yp[(int64_t)gy * W + gx] = b;
+        cp[(int64_t)gy * W + gx] = (unsigned char)(a * WX + RA[r0 + i + a][tx]);
+      }
+    }
+  }
+}
+
+// Backward from the saved codes: grad_in[q] = sum over the outputs p of q's window, in raster order
+// of p, of grad_out[p] when code(p) names q -- the gather of k_flat_bwd without recomputing the
+// codes.  A thread owns four consecutive outputs q of a row (a quad at columns 4t .. 4t + 3 of the
+// tile); for window row a the codes of all 4 x (2R+1) candidates p sit in the 4 + 2R bytes at staged
+// column 4t, read as whole 32-bit words.  For each candidate column b one funnel shift lines up the
+// four codes (one per q of the quad) and one exact zero-byte test of (codes ^ splat(want)) tells
+// which q of the quad p routes to -- usually none, and grad_out is read (a predicated load) only for
+// the matches.  (a, b)
+// run in raster order, so each q adds its contributions in the order of a sequential accumulation
+// in raster order of the outputs.  Codes outside the image are 255 and never match.
+static constexpr int AQ_QUADS = 64, AQ_ROWS = 4;  // 256 threads: 64 quads x 4 row groups
+template <int R>
+__global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char *__restrict__ code,
+                                                             const float *__restrict__ gy, float *__restrict__ gx,
+                                                             int H, int W) {
+  constexpr int WX = 2 * R + 1, TW = 4 * AQ_QUADS, SH = AT_H + 2 * R;
+  constexpr int SWW = AQ_QUADS + (2 * R + 3) / 4 + 1;  // staged code words per row (4 codes each)
+  constexpr int SW = 4 * SWW;                           // staged columns
+  __shared__ uint32_t C[SH][SWW];
+  __shared__ float G[SH][SW + 1];
+  const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * TW;
+  const int64_t plane = (int64_t)blockIdx.z * H * W;
+  const float *gp = gy + plane;
+  const unsigned char *cp = code + plane;
+  unsigned char *Cb = reinterpret_cast<unsigned char *>(&C[0][0]);
+  for (int i = threadIdx.x; i < SH * SW; i += AT_THREADS) {
+    const int r = i / SW, c = i - r * SW;
+    const int yy = ty0 - R + r, xx = tx0 - R + c;
+    const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
+    const int64_t o = in ? (int64_t)yy * W + xx : 0;
+    const float g = __ldg(gp + o);
+    const unsigned char k = __ldg(cp + o);
+    G[r][c] = in ? g : 0.f;
+    Cb[r * SW + c] = in ? k : (unsigned char)255;
+  }
+  __syncthreads();
+  const int t = threadIdx.x % AQ_QUADS, tq = threadIdx.x / AQ_QUADS;
+  const int xq = tx0 + 4 * t;  // the quad's first column
+  if (xq >= W) return;
+  float *op = gx + plane;
+  for (int r = tq; r < AT_H; r += AQ_ROWS) {
+    const int yy = ty0 + r;
+    if (yy >= H) break;
+    float sum[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int a = 0; a < WX; ++a) {
+      uint32_t w[(2 * R + 3) / 4 + 1];
+#pragma unroll
+      for (int k = 0; k < (2 * R + 3) / 4 + 1; ++k) w[k] = C[r + a][t + k];
+#pragma unroll
+      for (int b = 0; b < WX; ++b) {
+        // codes of the candidates at column b of window row a, for q = quad + 0..3
+        const uint32_t cw = (b % 4 == 0) ? w[b / 4] : __funnelshift_r(w[b / 4], w[b / 4 + 1], 8 * (b % 4));
+        const uint32_t want = 0x01010101u * (uint32_t)((2 * R - a) * WX + (2 * R - b));
+        const uint32_t x = cw ^ want;
+        const uint32_t z = ~((((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x) | 0x7f7f7f7fu);  // 0x80 in each zero byte
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (z & (0x80u << (8 * j))) sum[j] += G[r + a][4 * t + j + b];  // read only where it matched
+      }
+    }
+    float *o = op + (int64_t)yy * W + xq;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (xq + j < W) o[j] = sum[j];
+  }
+}
+
 template <bool SUP>
 static bool flat_fwd_fixed(const float *x, float *y, int64_t planes, int64_t h, int64_t w, int ry, int rx, cudaStream_t s) {
   if (ry != rx || ry < 1 || ry > 3 || planes > 65535) return false;
@@ -480,6 +632,39 @@ pg_status launch_flat2d(const float *x, float *y, int64_t planes, int64_t h, int
     k_flat_fwd<false><<<flat_grid(planes, h, w), AT_THREADS, sm, s>>>(x, y, planes, (int)h, (int)w, ry, rx);
   }
   return cuda_status(cudaGetLastError(), "flat morphology forward launch");
+}
+
+pg_status launch_flat2d_arg(const float *x, float *y, unsigned char *code, int64_t planes, int64_t h, int64_t w, int r,
+                            bool dilate, cudaStream_t s) {
+  if (r < 1 || r > 3) return fail(PG_ERR_INVALID_ARGUMENT, "saved-arg forward: square windows of half size 1 to 3");
+  if (planes * h * w == 0) return PG_OK;
+  if (h > (1 << 30) || w > (1 << 30) || ceil_div(h, AT_H) > 65535 || planes > 65535)
+    return fail(PG_ERR_INVALID_ARGUMENT, "plane too large");
+  const dim3 grid((unsigned)ceil_div(w, AF_TX - 2 * r), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
+  const int ih = (int)h, iw = (int)w;
+  if (dilate) {
+    if (r == 1) k_flat_fwd_arg<true, 1><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+    else if (r == 2) k_flat_fwd_arg<true, 2><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+    else k_flat_fwd_arg<true, 3><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+  } else {
+    if (r == 1) k_flat_fwd_arg<false, 1><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+    else if (r == 2) k_flat_fwd_arg<false, 2><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+    else k_flat_fwd_arg<false, 3><<<grid, AT_THREADS, 0, s>>>(x, y, code, ih, iw);
+  }
+  return cuda_status(cudaGetLastError(), "flat morphology forward (saved arg) launch");
+}
+
+pg_status launch_flat2d_backward_arg(const unsigned char *code, const float *gy, float *gx, int64_t planes, int64_t h,
+                                     int64_t w, int r, cudaStream_t s) {
+  if (r < 1 || r > 3) return fail(PG_ERR_INVALID_ARGUMENT, "saved-arg backward: square windows of half size 1 to 3");
+  if (planes * h * w == 0) return PG_OK;
+  if (h > (1 << 30) || w > (1 << 30) || ceil_div(h, AT_H) > 65535 || planes > 65535)
+    return fail(PG_ERR_INVALID_ARGUMENT, "plane too large");
+  const dim3 grid((unsigned)ceil_div(w, 4 * AQ_QUADS), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
+  if (r == 1) k_flat_bwd_arg<1><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
+  else if (r == 2) k_flat_bwd_arg<2><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
+  else k_flat_bwd_arg<3><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
+  return cuda_status(cudaGetLastError(), "flat morphology backward (saved arg) launch");
 }
 
 pg_status launch_flat2d_backward(const float *x, const float *gy, float *gx, int64_t planes, int64_t h, int64_t w,

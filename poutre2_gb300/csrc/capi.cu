@@ -819,4 +819,19 @@ pg_status pg_flat_morph2d_backward(const float *x, const float *gy, float *gx, i
   return launch_flat2d_backward(x, gy, gx, planes, h, w, ry, rx, dilate != 0, STREAM(s));
 }
 
+pg_status pg_flat_morph2d_forward_arg(const float *x, float *y, uint8_t *code, int64_t planes, int64_t h, int64_t w,
+                                      int32_t r, int32_t dilate, pg_stream_t s) {
+  if (planes < 0 || h < 0 || w < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative dimension");
+  if (planes * h * w > 0 && (!x || !y || !code)) return fail(PG_ERR_INVALID_ARGUMENT, "null tensor");
+  if (x == y && x) return fail(PG_ERR_ALIASING, "input output tensors must be different");
+  return launch_flat2d_arg(x, y, code, planes, h, w, r, dilate != 0, STREAM(s));
+}
+pg_status pg_flat_morph2d_backward_arg(const uint8_t *code, const float *gy, float *gx, int64_t planes, int64_t h,
+                                       int64_t w, int32_t r, pg_stream_t s) {
+  if (planes < 0 || h < 0 || w < 0) return fail(PG_ERR_INVALID_ARGUMENT, "negative dimension");
+  if (planes * h * w > 0 && (!code || !gy || !gx)) return fail(PG_ERR_INVALID_ARGUMENT, "null tensor");
+  if (gx && gx == gy) return fail(PG_ERR_ALIASING, "grad_in must be a distinct tensor");
+  return launch_flat2d_backward_arg(code, gy, gx, planes, h, w, r, STREAM(s));
+}
+
 }  // extern "C"

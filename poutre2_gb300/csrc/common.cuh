@@ -333,5 +333,9 @@ pg_status launch_flat2d(const float *x, float *y, int64_t planes, int64_t h, int
                         cudaStream_t s);
 pg_status launch_flat2d_backward(const float *x, const float *gy, float *gx, int64_t planes, int64_t h, int64_t w,
                                  int ry, int rx, bool dilate, cudaStream_t s);
+pg_status launch_flat2d_arg(const float *x, float *y, unsigned char *code, int64_t planes, int64_t h, int64_t w, int r,
+                            bool dilate, cudaStream_t s);
+pg_status launch_flat2d_backward_arg(const unsigned char *code, const float *gy, float *gx, int64_t planes, int64_t h,
+                                     int64_t w, int r, cudaStream_t s);
 
 }  // namespace pg
