@@ -328,7 +328,8 @@ PG_API pg_status pg_flat_morph2d_backward(const float *x, const float *grad_out,
 /* The same forward and adjoint for a square (2r+1) x (2r+1) window, r = 1..3, with the arg saved
  * instead of recomputed: the forward also writes code[p] = a*(2r+1) + b (one byte per pixel), the
  * window row a and column b of p's first-in-scan-order arg-extremum; the backward gathers from the
- * codes and grad_out alone.  y and grad_in are bit-identical to pg_flat_morph2d_forward / _backward. */
+ * codes and grad_out alone.  y is bit-identical to pg_flat_morph2d_forward; grad_in to
+ * pg_flat_morph2d_backward for every x without NaN. */
 PG_API pg_status pg_flat_morph2d_forward_arg(const float *x, float *y, uint8_t *code, int64_t planes, int64_t h,
                                              int64_t w, int32_t r, int32_t dilate, pg_stream_t stream);
 PG_API pg_status pg_flat_morph2d_backward_arg(const uint8_t *code, const float *grad_out, float *grad_in, int64_t planes,

@@ -216,18 +216,19 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_r(const float *__restri
 }
 
 // Forward that also saves each output's arg code for the backward: code(p) = a * (2R+1) + b, (a, b)
-// the window row and column of p's first-in-scan-order arg-extremum (the first strictly-best row of
-// the window, then that row's first strictly-best column, as k_flat_bwd computes them; 255 is never
-// written for an image pixel).  The values are the same best_of chains as k_flat_fwd_r, so y is
-// bit-identical to the plain forward.
+// the window row and column of p's first-in-scan-order arg-extremum.  The values are the best_of
+// chains of k_flat_fwd_r (y is bit-identical to the plain forward); the arg is the first position
+// equal to that value -- in the row pass the first column of each row window equal to its best, in the
+// column pass the first window row whose row-best equals the output.  Without NaN in x that is the
+// position the strictly-better chains of k_flat_bwd find (equal values, -0 and +0 included, compare
+// equal), so the backward from these codes is bit-identical to the recomputing one.
 template <bool SUP, int R>
 __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__restrict__ x, float *__restrict__ y,
                                                              unsigned char *__restrict__ code, int H, int W) {
   constexpr int FW = AF_TX - 2 * R, WX = 2 * R + 1;
   constexpr int XH = AT_H + 2 * R, XW = AF_TX;
   __shared__ float X[XH][XW + 1];
-  __shared__ float RV[XH][FW + 1];   // row-best values (best_of chain)
-  __shared__ float RB[XH][FW + 1];   // row-best values of the strict-better chain (equal to RV without NaN)
+  __shared__ float RV[XH][FW + 1];   // row-best values
   __shared__ unsigned char RA[XH][FW + 1];
   const int tx = threadIdx.x % AF_TX, tq = threadIdx.x / AF_TX;
   const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * FW;
@@ -255,16 +256,16 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__rest
     for (int k = 0; k < RI; ++k) {
       const int r = tq + k * AF_TY;
       if (r < XH) {
-        float b = X[r][tx], bb = b;
-        int a = 0;
+        float e[2 * R + 1];
 #pragma unroll
-        for (int d = 1; d <= 2 * R; ++d) {
-          const float v = X[r][tx + d];
-          b = best_of<SUP>(b, v);
-          if (better<SUP>(v, bb)) { bb = v; a = d; }
-        }
+        for (int d = 0; d <= 2 * R; ++d) e[d] = X[r][tx + d];
+        float b = e[0];
+#pragma unroll
+        for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, e[d]);
+        int a = 2 * R;
+#pragma unroll
+        for (int d = 2 * R - 1; d >= 0; --d) a = (e[d] == b) ? d : a;
         RV[r][tx] = b;
-        RB[r][tx] = bb;
         RA[r][tx] = (unsigned char)a;
       }
     }
@@ -275,21 +276,17 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__rest
     unsigned char *cp = code + plane;
     constexpr int OR = AT_H / AF_TY;
     const int r0 = tq * OR, gx = tx0 + tx;
-    float col[OR + 2 * R], colb[OR + 2 * R];
+    float col[OR + 2 * R];
 #pragma unroll
-    for (int i = 0; i < OR + 2 * R; ++i) {
-      col[i] = RV[r0 + i][tx];
-      colb[i] = RB[r0 + i][tx];
-    }
+    for (int i = 0; i < OR + 2 * R; ++i) col[i] = RV[r0 + i][tx];
 #pragma unroll
     for (int i = 0; i < OR; ++i) {
-      float b = col[i], bb = colb[i];
-      int a = 0;
+      float b = col[i];
 #pragma unroll
-      for (int d = 1; d <= 2 * R; ++d) {
-        b = best_of<SUP>(b, col[i + d]);
-        if (better<SUP>(colb[i + d], bb)) { bb = colb[i + d]; a = d; }
-      }
+      for (int d = 1; d <= 2 * R; ++d) b = best_of<SUP>(b, col[i + d]);
+      int a = 2 * R;
+#pragma unroll
+      for (int d = 2 * R - 1; d >= 0; --d) a = (col[i + d] == b) ? d : a;
       const int gy = ty0 + r0 + i;
       if (gy < H && gx < W) {
         yp[(int64_t)gy * W + gx] = b;
