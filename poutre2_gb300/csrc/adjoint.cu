@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__rest
 // tile); for window row a the codes of all 4 x (2R+1) candidates p sit in the 4 + 2R bytes at staged
 // column 4t, read as whole 32-bit words.  For each candidate column b one funnel shift lines up the
 // four codes (one per q of the quad) and one exact zero-byte test of (codes ^ splat(want)) tells
-// which q of the quad p routes to -- usually none, and grad_out is read (a predicated load) only for
-// the matches.  (a, b)
+// which q of the quad p routes to -- usually none; grad_out of the window row comes in as whole
+// 16-byte vectors and is added only where the code matched.  (a, b)
 // run in raster order, so each q adds its contributions in the order of a sequential accumulation
 // in raster order of the outputs.  Codes outside the image are 255 and never match.
 static constexpr int AQ_QUADS = 64, AQ_ROWS = 4;  // 256 threads: 64 quads x 4 row groups
@@ -314,8 +314,9 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char
   constexpr int WX = 2 * R + 1, TW = 4 * AQ_QUADS, SH = AT_H + 2 * R;
   constexpr int SWW = AQ_QUADS + (2 * R + 3) / 4 + 1;  // staged code words per row (4 codes each)
   constexpr int SW = 4 * SWW;                           // staged columns
+  constexpr int GV = (2 * R + 3) / 4 + 1;               // float4 of grad_out per window row and quad
   __shared__ uint32_t C[SH][SWW];
-  __shared__ float G[SH][SW + 1];
+  __shared__ __align__(16) float G[SH][SW];
   const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * TW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *gp = gy + plane;
@@ -342,9 +343,14 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char
     float sum[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int a = 0; a < WX; ++a) {
-      uint32_t w[(2 * R + 3) / 4 + 1];
+      uint32_t w[GV];
+      float g[4 * GV];  // grad_out of the quad's candidate columns 4t .. 4t + 4GV - 1 of window row a
 #pragma unroll
-      for (int k = 0; k < (2 * R + 3) / 4 + 1; ++k) w[k] = C[r + a][t + k];
+      for (int k = 0; k < GV; ++k) {
+        w[k] = C[r + a][t + k];
+        const float4 v = *reinterpret_cast<const float4 *>(&G[r + a][4 * (t + k)]);
+        g[4 * k] = v.x; g[4 * k + 1] = v.y; g[4 * k + 2] = v.z; g[4 * k + 3] = v.w;
+      }
 #pragma unroll
       for (int b = 0; b < WX; ++b) {
         // codes of the candidates at column b of window row a, for q = quad + 0..3
@@ -354,7 +360,7 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char
         const uint32_t z = ~((((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x) | 0x7f7f7f7fu);  // 0x80 in each zero byte
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (z & (0x80u << (8 * j))) sum[j] += G[r + a][4 * t + j + b];  // read only where it matched
+          if (z & (0x80u << (8 * j))) sum[j] += g[b + j];
       }
     }
     float *o = op + (int64_t)yy * W + xq;
