@@ -12,6 +12,8 @@
 // once and every output byte written once.  The horizontal 3-neighbourhood of a pack comes
 // from its two edge neighbours (one scalar load each, L1 hits) and a funnel shift;
 // u8/u16 use the SIMD-in-word min/max.
+#include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "common.cuh"
@@ -236,15 +238,49 @@ static int rows_per_thread(int64_t threads_without_strips, int64_t length, int c
   return (int)r;
 }
 
+// CTAs of 256 threads of kernel KERN that fit on the GPU at once (cached per kernel)
+template <auto KERN> static int64_t resident_ctas() {
+  static std::atomic<int> cached{0};
+  int v = cached.load();
+  if (v == 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, KERN, 256, 0) != cudaSuccess || per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    v = per_sm * num_sms();
+    cached.store(v);
+  }
+  return v;
+}
+
+// Rows (slices) per thread: the fewest that keep the grid within one wave of resident CTAs, so that
+// no short second wave runs alone (4096^2 u8: 688 CTAs on 608 slots before, 1.13 waves); images too
+// large for that at `cap` rows per thread run several full waves at the heuristic's length.
+template <typename F> static int strip_rows(int64_t length, int cap, int64_t slots, int heuristic, F ctas_for) {
+  int lo = 1, hi = (int)std::min<int64_t>(cap, std::max<int64_t>(length, 1));
+  if (ctas_for(hi) > slots) return heuristic;
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (ctas_for(mid) <= slots) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
 template <typename T, bool SUP, int SHAPE>
 static pg_status small2d_t(const T *in, T *out, int64_t H, int64_t W, cudaStream_t s) {
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
   const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
-  const int R = rows_per_thread(npack, H, 32);
   const int bx = npack >= 32 ? 32 : npack >= 16 ? 16 : npack >= 8 ? 8 : npack >= 4 ? 4 : npack >= 2 ? 2 : 1;
+  const int64_t gx = ceil_div(npack, bx);
+  const int64_t slots = vec ? resident_ctas<k_small2d<T, SUP, SHAPE, typename PackOf<T>::type>>()
+                            : resident_ctas<k_small2d<T, SUP, SHAPE, Scalar<T>>>();
+  const int R = strip_rows(H, 32, slots, rows_per_thread(npack, H, 32),
+                           [&](int r) { return gx * ceil_div(ceil_div(H, r), 256 / bx); });
   dim3 block(bx, 256 / bx);
-  dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(ceil_div(H, R), 256 / bx));
+  dim3 grid((unsigned)gx, (unsigned)ceil_div(ceil_div(H, R), 256 / bx));
   if (grid.y > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "image too tall for the small-SE kernel");
   if (vec) k_small2d<T, SUP, SHAPE, typename PackOf<T>::type><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
   else k_small2d<T, SUP, SHAPE, Scalar<T>><<<grid, block, 0, s>>>(in, out, H, W, npack, R);
@@ -256,9 +292,12 @@ static pg_status small3d_t(const T *in, T *out, int64_t D, int64_t H, int64_t W,
   const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) % 16 == 0);
   const bool vec = aligned && (W % Pack<T>::N == 0);
   const int64_t npack = vec ? W / Pack<T>::N : W;
-  const int R = rows_per_thread(npack * H, D, 16);
   // no idle lanes when a row holds fewer than 32 packs
   const int bx = npack >= 32 ? 32 : npack >= 16 ? 16 : npack >= 8 ? 8 : npack >= 4 ? 4 : npack >= 2 ? 2 : 1;
+  const int64_t gxy = ceil_div(npack, bx) * ceil_div(H, 256 / bx);
+  const int64_t slots = vec ? resident_ctas<k_small3d<T, SUP, SHAPE, typename PackOf<T>::type>>()
+                            : resident_ctas<k_small3d<T, SUP, SHAPE, Scalar<T>>>();
+  const int R = strip_rows(D, 16, slots, rows_per_thread(npack * H, D, 16), [&](int r) { return gxy * ceil_div(D, r); });
   dim3 block(bx, 256 / bx);
   dim3 grid((unsigned)ceil_div(npack, bx), (unsigned)ceil_div(H, 256 / bx), (unsigned)ceil_div(D, R));
   if (grid.y > 65535 || grid.z > 65535) return fail(PG_ERR_INVALID_ARGUMENT, "volume too large for the small-SE kernel");
