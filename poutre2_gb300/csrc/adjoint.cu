@@ -307,30 +307,46 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_fwd_arg(const float *__rest
 // run in raster order, so each q adds its contributions in the order of a sequential accumulation
 // in raster order of the outputs.  Codes outside the image are 255 and never match.
 static constexpr int AQ_QUADS = 64, AQ_ROWS = 4;  // 256 threads: 64 quads x 4 row groups
+// The staged band starts 4 columns left of the tile (a 16-byte boundary when rows are whole 16-byte
+// vectors), so logical column c -- tile column c - R -- sits at staged column c + 4 - R.
 template <int R>
 __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char *__restrict__ code,
                                                              const float *__restrict__ gy, float *__restrict__ gx,
-                                                             int H, int W) {
-  constexpr int WX = 2 * R + 1, TW = 4 * AQ_QUADS, SH = AT_H + 2 * R;
-  constexpr int SWW = AQ_QUADS + (2 * R + 3) / 4 + 1;  // staged code words per row (4 codes each)
-  constexpr int SW = 4 * SWW;                           // staged columns
-  constexpr int GV = (2 * R + 3) / 4 + 1;               // float4 of grad_out per window row and quad
+                                                             int H, int W, int vec) {
+  constexpr int WX = 2 * R + 1, TW = 4 * AQ_QUADS, SH = AT_H + 2 * R, OFF = 4 - R;
+  constexpr int GV = (OFF + 2 * R + 3) / 4 + 1;  // words / float4s per window row and quad
+  constexpr int SWW = AQ_QUADS + GV;             // staged words (4 codes, or 4 floats) per row
+  constexpr int SW = 4 * SWW;
   __shared__ uint32_t C[SH][SWW];
   __shared__ __align__(16) float G[SH][SW];
   const int ty0 = blockIdx.y * AT_H, tx0 = blockIdx.x * TW;
   const int64_t plane = (int64_t)blockIdx.z * H * W;
   const float *gp = gy + plane;
   const unsigned char *cp = code + plane;
-  unsigned char *Cb = reinterpret_cast<unsigned char *>(&C[0][0]);
-  for (int i = threadIdx.x; i < SH * SW; i += AT_THREADS) {
-    const int r = i / SW, c = i - r * SW;
-    const int yy = ty0 - R + r, xx = tx0 - R + c;
-    const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
-    const int64_t o = in ? (int64_t)yy * W + xx : 0;
-    const float g = __ldg(gp + o);
-    const unsigned char k = __ldg(cp + o);
-    G[r][c] = in ? g : 0.f;
-    Cb[r * SW + c] = in ? k : (unsigned char)255;
+  if (vec) {
+    // whole 16-byte groups of 4 columns, each wholly inside or outside the image
+    for (int i = threadIdx.x; i < SH * SWW; i += AT_THREADS) {
+      const int r = i / SWW, m = i - r * SWW;
+      const int yy = ty0 - R + r, xx = tx0 - 4 + 4 * m;
+      const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const int64_t o = in ? (int64_t)yy * W + xx : 0;
+      const float4 g = __ldg(reinterpret_cast<const float4 *>(gp + o));
+      const uint32_t k = __ldg(reinterpret_cast<const unsigned int *>(cp + o));
+      *reinterpret_cast<float4 *>(&G[r][4 * m]) = in ? g : make_float4(0.f, 0.f, 0.f, 0.f);
+      C[r][m] = in ? k : 0xffffffffu;
+    }
+  } else {
+    unsigned char *Cb = reinterpret_cast<unsigned char *>(&C[0][0]);
+    for (int i = threadIdx.x; i < SH * SW; i += AT_THREADS) {
+      const int r = i / SW, c = i - r * SW;
+      const int yy = ty0 - R + r, xx = tx0 - 4 + c;
+      const bool in = yy >= 0 && yy < H && xx >= 0 && xx < W;
+      const int64_t o = in ? (int64_t)yy * W + xx : 0;
+      const float g = __ldg(gp + o);
+      const unsigned char k = __ldg(cp + o);
+      G[r][c] = in ? g : 0.f;
+      Cb[r * SW + c] = in ? k : (unsigned char)255;
+    }
   }
   __syncthreads();
   const int t = threadIdx.x % AQ_QUADS, tq = threadIdx.x / AQ_QUADS;
@@ -344,7 +360,7 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char
 #pragma unroll
     for (int a = 0; a < WX; ++a) {
       uint32_t w[GV];
-      float g[4 * GV];  // grad_out of the quad's candidate columns 4t .. 4t + 4GV - 1 of window row a
+      float g[4 * GV];  // grad_out of staged columns 4t .. 4t + 4GV - 1 of window row a
 #pragma unroll
       for (int k = 0; k < GV; ++k) {
         w[k] = C[r + a][t + k];
@@ -353,14 +369,16 @@ __global__ void __launch_bounds__(AT_THREADS) k_flat_bwd_arg(const unsigned char
       }
 #pragma unroll
       for (int b = 0; b < WX; ++b) {
-        // codes of the candidates at column b of window row a, for q = quad + 0..3
-        const uint32_t cw = (b % 4 == 0) ? w[b / 4] : __funnelshift_r(w[b / 4], w[b / 4 + 1], 8 * (b % 4));
+        // codes of the candidates at column b of window row a (staged column 4t + OFF + b + j), for
+        // q = quad + j, j = 0..3
+        const int sb = OFF + b;
+        const uint32_t cw = (sb % 4 == 0) ? w[sb / 4] : __funnelshift_r(w[sb / 4], w[sb / 4 + 1], 8 * (sb % 4));
         const uint32_t want = 0x01010101u * (uint32_t)((2 * R - a) * WX + (2 * R - b));
         const uint32_t x = cw ^ want;
         const uint32_t z = ~((((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x) | 0x7f7f7f7fu);  // 0x80 in each zero byte
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (z & (0x80u << (8 * j))) sum[j] += g[b + j];
+          if (z & (0x80u << (8 * j))) sum[j] += g[sb + j];
       }
     }
     float *o = op + (int64_t)yy * W + xq;
@@ -664,9 +682,12 @@ pg_status launch_flat2d_backward_arg(const unsigned char *code, const float *gy,
   if (h > (1 << 30) || w > (1 << 30) || ceil_div(h, AT_H) > 65535 || planes > 65535)
     return fail(PG_ERR_INVALID_ARGUMENT, "plane too large");
   const dim3 grid((unsigned)ceil_div(w, 4 * AQ_QUADS), (unsigned)ceil_div(h, AT_H), (unsigned)planes);
-  if (r == 1) k_flat_bwd_arg<1><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
-  else if (r == 2) k_flat_bwd_arg<2><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
-  else k_flat_bwd_arg<3><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w);
+  // 16-byte staging: rows of whole vectors (4 floats, 4 codes) and aligned bases
+  const int vec = (w % 4 == 0 && reinterpret_cast<uintptr_t>(gy) % 16 == 0 && reinterpret_cast<uintptr_t>(code) % 4 == 0)
+                      ? 1 : 0;
+  if (r == 1) k_flat_bwd_arg<1><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w, vec);
+  else if (r == 2) k_flat_bwd_arg<2><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w, vec);
+  else k_flat_bwd_arg<3><<<grid, AT_THREADS, 0, s>>>(code, gy, gx, (int)h, (int)w, vec);
   return cuda_status(cudaGetLastError(), "flat morphology backward (saved arg) launch");
 }
 
