@@ -143,6 +143,10 @@ static pg_status check_scalar(int ptype, const pg_scalar *v, const char *what) {
 // `iter` passes of a small static SE, alternating between `out` and a temporary
 static pg_status repeat_small(const pg_image &in, int se, int iter, const pg_image &out, bool dilate, cudaStream_t s) {
   if (iter == 1) return launch_small_se(in, out, se, dilate, s);
+  if (se == PG_SE_CROSS_2D && in.rank == 2) {  // the iterated cross: all passes in one tile kernel (octagon.cu)
+    pg_status st = PG_OK;
+    if (try_octagon_tile(in, out, iter, 0, dilate, s, &st)) return st;
+  }
   Scratch tmp;
   PG_TRY(tmp.alloc((size_t)dims_of(in).count() * elem_size(in.ptype), s));
   pg_image t = in;

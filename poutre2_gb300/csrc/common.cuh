@@ -267,8 +267,9 @@ bool try_segment_open(const pg_image &in, const pg_image &out, int dy, int dx, i
 bool try_segment_gradient(const pg_image &in, const pg_image &out, int dy, int dx, int k, cudaStream_t s,
                           pg_status *st);  // dilation - erosion by that segment in one pass
 int take_diag_status();  // device status of the diagonal tile kernel since the last call (0: none)
-// The octagon's n = n_cross + n_square passes (2 <= n <= 16) in one shared-memory tile kernel
-// (octagon.cu): u8 and u16 images with rows of a multiple of 16 bytes.
+// The octagon's n = n_cross + n_square passes in one shared-memory tile kernel (octagon.cu): u8 images
+// for 5 <= n <= 16, u16 for 3 <= n <= 16, rows of a multiple of 16 bytes.  n_square = 0: the cross
+// iterated n times (SECross2D, iter = n).
 bool try_octagon_tile(const pg_image &in, const pg_image &out, int n_cross, int n_square, bool dilate, cudaStream_t s,
                       pg_status *st);
 int take_oct_status();  // device status of the octagon tile kernel since the last call (0: none)

@@ -1,5 +1,6 @@
 """The octagon's passes in one shared-memory tile kernel (csrc/octagon.cu): u8 and u16 images with rows
-of a multiple of 16 bytes, sizes 2..16, dilation and erosion, against the oracle's compound
+of a multiple of 16 bytes, sizes 2..16 (the tile from 5 passes for u8, from 3 for u16; fewer take the
+separate passes), dilation and erosion, against the oracle's compound
 Erode / Dilate (ero_dil_compound_static_se_t.hpp:34-160, pinned against poutre2's compound path).
 The shapes put tile columns (56 / 48 words), tile rows (128 - 2n) and the image border in every
 relative position: one row, one 16-byte column, images smaller than a tile, several tiles across and
@@ -17,7 +18,7 @@ SHAPES = {np.uint8: [(1, 16), (3, 32), (17, 48), (96, 224), (110, 240), (127, 40
 
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16])
-@pytest.mark.parametrize("size", [2, 3, 5, 8, 9, 12, 16])
+@pytest.mark.parametrize("size", [2, 3, 4, 5, 8, 9, 12, 16])
 def test_octagon_tile_matches_the_compound_passes(dt, size):
     from poutre2_gb300 import llm
     from poutre2_gb300.se import Compound_NL_SE
@@ -30,6 +31,24 @@ def test_octagon_tile_matches_the_compound_passes(dt, size):
             (llm.Dilate if dil else llm.Erode)(x, Compound_NL_SE.Octagon, size, out)
             np.testing.assert_array_equal(out.cpu().numpy(), oracle.erode_dilate_compound(a, "Octagon", size, dil),
                                           err_msg=f"{shape} size={size} dilate={dil}")
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+def test_iterated_cross_takes_the_tile_kernel(dt):
+    """Erode / Dilate by SECross2D iterated 2..16 times (the diamond) in one tile launch, against the
+    oracle's iterated passes (ero_dil_static.cpp:229-306)."""
+    from poutre2_gb300 import llm
+    from poutre2_gb300.se import Common_NL_SE
+    rng = np.random.default_rng(77 + np.dtype(dt).itemsize)
+    for shape in SHAPES[dt]:
+        a = rng.integers(0, np.iinfo(dt).max + 1, shape).astype(dt)
+        x = torch.from_numpy(a).cuda()
+        for it in (2, 3, 5, 7, 16):
+            for dil in (True, False):
+                out = torch.full_like(x, 7)
+                (llm.Dilate if dil else llm.Erode)(x, Common_NL_SE.SECross2D, it, out)
+                np.testing.assert_array_equal(out.cpu().numpy(), oracle.erode_dilate_static(a, "SECross2D", it, dil),
+                                              err_msg=f"{shape} iter={it} dilate={dil}")
 
 
 def test_octagon_tile_large_image_status_clean():
