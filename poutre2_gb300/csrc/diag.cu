@@ -14,10 +14,12 @@
 // staircase of TMA boxes: the rows are cut into groups of G = 16 / sizeof(T) rows, the drift of one
 // 16-byte chunk, and group g is one 2D box of G rows x (TW + G) pixels that starts G pixels further
 // left (45 degrees) or right (135 degrees) than group g - 1 -- for the vertical segment one box of TW
-// pixels holds all rows.  Every box starts on a 16-byte boundary, the tile rows start on a multiple of
-// G, and in shared memory line t at row k of a group sits at column t + G - k (45 degrees), t + k (135)
-// or t (vertical).  Pixels outside the image arrive as TMA's zero fill and are then set to the first
-// operator's neutral value (nothing to do when that is 0: the dilation of unsigned pixels).
+// pixels holds all rows, and a 45-degree tile whose columns all lie in the image takes the whole
+// staircase as one box of a sheared 3D view of the image.  Every box starts on a 16-byte boundary, the
+// tile rows start on a multiple of G, and in shared memory line t at row k of a group sits at column
+// t + G - k (45 degrees), t + k (135) or t (vertical).  Pixels outside the image arrive as TMA's zero
+// fill and are then set to the first operator's neutral value (nothing to do when that is 0: the
+// dilation of unsigned pixels).
 //
 // Each thread runs van Herk / Gil-Werman down one line: the CH windows starting at tile rows R0 .. R0 +
 // CH - 1 (CH the largest multiple of G <= 2K + 1, R0 a multiple of G) take the running suffix of block
@@ -205,8 +207,11 @@ __global__ void __launch_bounds__(DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>:
   if (!s_ok) return;
   // 45 degrees: the whole staircase is one box of the sheared view `smap` (group j of the view starts
   // 16 bytes left of row G*j, so view column X of group j is image column X - G*j), unless the tile
-  // reaches the last H mod G rows, which the view leaves out (shear_rows = G * floor(H / G))
-  const bool sheared = DIR > 0 && shear_rows > 0 && (shear_rows == H || ty + BR <= shear_rows);
+  // reaches the last H mod G rows, which the view leaves out (shear_rows = G * floor(H / G)), or a
+  // side of the image, where the view would bring pixels of the neighbouring rows instead of the 2D
+  // boxes' zero fill
+  const bool sheared = DIR > 0 && shear_rows > 0 && (shear_rows == H || ty + BR <= shear_rows) &&
+                       box_x(BR / G - 1) >= 0 && box_x(0) + BWP <= W;
   if (sheared) {
     if (tid == 0)
       asm volatile(
@@ -235,15 +240,13 @@ __global__ void __launch_bounds__(DiagGeom<T, K, DIR, (MODE == 2 || MODE == 3)>:
   if (!s_ok) return;
   (void)mbar_try(bar_a, 0);  // the phase is complete: each thread observes it (acquire)
 
-  // pixels outside the image: the 2D boxes hold TMA's zero fill there, the sheared view zeros above and
-  // below the image but, left and right of it, pixels of the neighbouring rows; the first operator
-  // needs its neutral value at all of them (zero already is it for the dilation of unsigned pixels,
-  // unless the sheared view brought neighbouring rows in)
-  if constexpr (!GRAD) {
+  // pixels outside the image: TMA's zero fill (the sheared view is used only where no column is outside
+  // the image); the first operator needs its neutral value there -- zero already is it for the dilation
+  // of unsigned pixels
+  if constexpr (!GRAD && !(std::is_unsigned_v<T> && SUP_A)) {
     const int xa = box_x(0), xb = box_x(BR / G - 1);
     const int xlo = DIR > 0 ? xb : xa, xhi = (DIR > 0 ? xa : xb) + BWP;
-    constexpr bool zero_neutral = std::is_unsigned_v<T> && SUP_A;
-    if ((!zero_neutral && (ty < 0 || ty + BR > H || xlo < 0 || xhi > W)) || (zero_neutral && sheared && (xlo < 0 || xhi > W))) {
+    if (ty < 0 || ty + BR > H || xlo < 0 || xhi > W) {
       const T NEU = OA::neutral();
       for (int r = tid; r < BR; r += Gm::NT) {
         const int g = r / G;
@@ -399,7 +402,8 @@ pg_status pixel_map(CUtensorMap *map, const void *data, int64_t H, int64_t W, in
 // X - G*j, with j < floor(H / G) and X < W + G*(floor(H / G) - 1).  Every coordinate inside those
 // bounds addresses a pixel of the image buffer: the largest is row G*floor(H/G) - 1 <= H - 1 at a
 // column <= W - 1, the smallest the first pixel, so the view reads nothing outside the buffer; left and
-// right of the image it reads pixels of the neighbouring rows, which the kernel then overwrites.  Box:
+// right of the image it would read pixels of the neighbouring rows, so tiles reaching a side use the 2D
+// boxes.  Box:
 // bw pixels x G rows x groups.  False if the driver refuses the view (the kernel then uses 2D boxes).
 bool sheared_map(CUtensorMap *map, const void *data, int64_t H, int64_t W, int S, int bw, int G, int groups) {
   auto fn = encode_tiled();
