@@ -4,7 +4,8 @@
 // Same result as line.cu / line_w.cu for the Y segment of 2K+1 pixels (DilateY/ErodeY,
 // ero_dil_line_se_t.hpp:249-282; clipped window) and for the 45 / 135 degree segments (runtime
 // neighbour lists).  Used for the half lengths instantiated below, 1/2/4-byte pixels, word-aligned
-// rows (the 1-/2-byte diagonals through k_dline_words, which keeps whole words).
+// rows (the 1-/2-byte diagonals through k_dline_words, which keeps whole words), where the TMA tiles of
+// diag.cu do not apply (their half lengths 7, 15, 31 on rows of a multiple of 16 bytes take those).
 //
 // A thread owns one 32-bit word column (E = 4/sizeof(T) adjacent pixel columns) of a strip of
 // rows and walks down it block by block (blocks of W = 2K+1 rows, anchored K rows above the
