@@ -273,6 +273,10 @@ int take_diag_status();  // device status of the diagonal tile kernel since the 
 bool try_octagon_tile(const pg_image &in, const pg_image &out, int n_cross, int n_square, bool dilate, cudaStream_t s,
                       pg_status *st);
 int take_oct_status();  // device status of the octagon tile kernel since the last call (0: none)
+// 3x3 square / cross and 3-pixel X / Y segments on TMA tiles (small_tile.cu): 2D u8 / u16 images with
+// rows of a multiple of 16 bytes.
+bool try_small_tile(const pg_image &in, const pg_image &out, int se, bool dilate, cudaStream_t s, pg_status *st);
+int take_small_tile_status();  // device status of the small-SE tile kernel since the last call (0: none)
 pg_status launch_rect(const pg_image &in, const pg_image &out, int64_t hy, int64_t hx, bool dilate, cudaStream_t s);
 // One-pass box (rect.cu): (hy, hx) = (k, k), (0, k) or (k, 0), k in {7, 15, 31}; 2-/4-byte pixels,
 // rows of a multiple of 16 bytes.  try_rect_gradient: dilation - erosion in the same pass.

@@ -1657,6 +1657,8 @@ pg_status pg_check_device(pg_stream_t stream) {
     return pg::fail(static_cast<pg_status>(ds), "a segment tile load did not complete within its wait limit");
   if (const int os8 = pg::take_oct_status())
     return pg::fail(static_cast<pg_status>(os8), "an octagon tile load did not complete within its wait limit");
+  if (const int ss = pg::take_small_tile_status())
+    return pg::fail(static_cast<pg_status>(ss), "a small-SE tile load did not complete within its wait limit");
   if (const int os = pg::take_open_status())
     return pg::fail(static_cast<pg_status>(os), "an opening tile load did not complete within its wait limit");
   if (const int ls = pg::take_label_status())

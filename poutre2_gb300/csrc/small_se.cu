@@ -329,6 +329,8 @@ static pg_status small_dispatch(const pg_image &in, const pg_image &out, int se,
 
 pg_status launch_small_se(const pg_image &in, const pg_image &out, int se, bool dilate, cudaStream_t s) {
   if (dims_of(in).count() == 0) return PG_OK;  // nothing to compute (and no empty grid to launch)
+  pg_status st;
+  if (try_small_tile(in, out, se, dilate, s, &st)) return st;
   PG_DISPATCH_PTYPE(in.ptype, T, {
     return dilate ? small_dispatch<T, true>(in, out, se, s) : small_dispatch<T, false>(in, out, se, s);
   });

@@ -260,12 +260,13 @@ __device__ __forceinline__ void col_scan(const uint32_t *ca, const uint32_t *cb,
 }
 
 
-// TMA copy of the box at word tx, row ty into s (bytes long), completing on the mbarrier `bar`;
-// thread 0 waits at most kWaitNs and records PG_ERR_CUDA in *status on expiry (and refuses to copy
-// into an s that is not 128-byte aligned).  Returns, for every
-// thread of the CTA, whether the tile arrived (one __syncthreads inside).
-__device__ __forceinline__ bool load_tile(const CUtensorMap *map, uint32_t *s, uint64_t *bar, unsigned bytes, int tx,
-                                          int ty, int *status, int *s_ok) {
+// TMA copy of the box at word tx, row ty (slice tz for a 3D map) into s (bytes long), completing on
+// the mbarrier `bar`; thread 0 waits at most kWaitNs and records PG_ERR_CUDA in *status on expiry (and
+// refuses to copy into an s that is not 128-byte aligned).  Returns, for every thread of the CTA,
+// whether the tile arrived (one __syncthreads inside).
+template <int NDIM = 2>
+__device__ __forceinline__ bool load_box(const CUtensorMap *map, uint32_t *s, uint64_t *bar, unsigned bytes, int tx,
+                                         int ty, int tz, int *status, int *s_ok) {
   const unsigned bar_a = smem_u32(bar);
   if (threadIdx.x == 0 && (smem_u32(s) & 127u)) {  // a TMA destination starts on a 128-byte boundary
     atomicCAS(status, 0, (int)PG_ERR_CUDA);
@@ -274,11 +275,18 @@ __device__ __forceinline__ bool load_tile(const CUtensorMap *map, uint32_t *s, u
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(bytes) : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(s)),
-        "l"(map), "r"(tx), "r"(ty), "r"(bar_a)
-        : "memory");
+    if constexpr (NDIM == 2)
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+              smem_u32(s)),
+          "l"(map), "r"(tx), "r"(ty), "r"(bar_a)
+          : "memory");
+    else
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+              smem_u32(s)),
+          "l"(map), "r"(tx), "r"(ty), "r"(tz), "r"(bar_a)
+          : "memory");
     bool done = mbar_try(bar_a, 0);
     const unsigned long long t0 = now_ns();
     while (!done && now_ns() - t0 < kWaitNs) done = mbar_try(bar_a, 0);
@@ -289,6 +297,11 @@ __device__ __forceinline__ bool load_tile(const CUtensorMap *map, uint32_t *s, u
   if (!*s_ok) return false;
   (void)mbar_try(bar_a, 0);  // the phase is complete: each thread observes it (acquire)
   return true;
+}
+
+__device__ __forceinline__ bool load_tile(const CUtensorMap *map, uint32_t *s, uint64_t *bar, unsigned bytes, int tx,
+                                          int ty, int *status, int *s_ok) {
+  return load_box<2>(map, s, bar, bytes, tx, ty, 0, status, s_ok);
 }
 
 inline PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
@@ -318,6 +331,22 @@ inline pg_status word_map(CUtensorMap *map, const void *data, int64_t H, int64_t
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the image tile");
+  return PG_OK;
+}
+
+// Tensor map of a volume of D slices x H rows x Wn 32-bit words, box of bw words x rows x slices.
+inline pg_status word_map3(CUtensorMap *map, const void *data, int64_t D, int64_t H, int64_t Wn, int bw, int rows,
+                           int slices) {
+  auto fn = encode_tiled();
+  if (!fn) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  cuuint64_t dims[3] = {(cuuint64_t)Wn, (cuuint64_t)H, (cuuint64_t)D};
+  cuuint64_t strides[2] = {(cuuint64_t)Wn * 4, (cuuint64_t)(Wn * H) * 4};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)rows, (cuuint32_t)slices};
+  cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void *>(data), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the volume tile");
   return PG_OK;
 }
 
