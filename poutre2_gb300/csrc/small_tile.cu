@@ -9,16 +9,16 @@
 // (by BZ slices for a volume).  One TMA copy brings the box around it -- a 16-byte chunk of halo left
 // and right, a row above and below, a slice before and after -- into shared memory, so all of the
 // tile's loads are in flight at once; the grids of the usual image sizes fit in one wave of resident
-// CTAs.  Thread (c, g) owns word column c over rows g * BY / 4 .. (g + 1) * BY / 4 - 1 (of every slice
-// of the tile): the left and right neighbours of each pixel come from funnel shifts with the
-// neighbouring words, the rows above and below are the next shared-memory rows, and a volume's slices
-// slide through registers.  u16 words are min / max'ed as u16x2; u8 words are split once into their
-// even and odd pixels on 16-bit lanes (the native u16x2 min / max; the packed 8-bit form is emulated),
-// combined there and merged once; i32 / f32 words hold one pixel.  Pixels outside the image arrive as
-// TMA's zero fill, the neutral value of the unsigned dilations; for the other operators, tiles at the
-// border set them to the neutral value first.  The TMA
-// wait is bounded (tile::kWaitNs); on expiry the CTA records PG_ERR_CUDA in g_small_tile_status (read
-// by pg_check_device) and leaves its tile unwritten.
+// CTAs.  A thread owns one word column (or, for u8 images, a 16-byte quad of words) over a run of the
+// tile's rows (of every slice of the tile): the left and right neighbours of each pixel come from
+// funnel shifts with the neighbouring words, the rows above and below are the next shared-memory
+// rows, and a volume's slices slide through registers.  u16 words are min / max'ed as u16x2; u8 words
+// are split once into their even and odd pixels on 16-bit lanes (the native u16x2 min / max; the
+// packed 8-bit form is emulated), combined there and merged once; i32 / f32 words hold one pixel.
+// Pixels outside the image arrive as TMA's zero fill, the neutral value of the unsigned dilations;
+// for the other operators, tiles at the border set them to the neutral value first.  The TMA wait is
+// bounded (tile::kWaitNs); on expiry the CTA records PG_ERR_CUDA in g_small_tile_status (read by
+// pg_check_device) and leaves its tile unwritten.
 #include "tile.cuh"
 
 namespace pg {
@@ -31,7 +31,11 @@ using namespace tile;
 constexpr int kSTThreads = 256;
 constexpr int kSTW = 64;         // output words per tile row
 constexpr int kSTBW = kSTW + 8;  // box words: one 16-byte chunk of halo each side
-constexpr int kST2Rows = 64;     // output rows of a 2D tile
+constexpr int kST2Rows = 64;     // output rows of a 2D tile (a thread per word)
+constexpr int kST2QRows = 128;   // output rows of a 2D tile (a thread per quad of words)
+// u8 images take the quad kernel (4096^2 square 12.3 -> 10.2 us); for u16 / i32 / f32 the thread per
+// word measured 1-2 % faster on 8192^2 / 16384^2 images and the same on 4096^2
+template <typename T> constexpr bool kQuad2D = sizeof(T) == 1;
 constexpr int kST3Rows = 16;     // output rows of a 3D tile
 constexpr int kST3Slices = 8;    // output slices of a 3D tile
 enum { ST_SQUARE = 0, ST_CROSS = 1, ST_SEGX = 2, ST_SEGY = 3, ST_SEGZ = 4 };
@@ -47,6 +51,19 @@ template <bool SUP> struct Lanes<uint16_t, SUP> {
   static __device__ __forceinline__ Lanes hor(const uint32_t *p) {
     const uint32_t w = p[0];
     return {m16<SUP>(w, m16<SUP>(__funnelshift_l(p[-1], w, 16), __funnelshift_r(w, p[1], 16)))};
+  }
+  // the four words from p (16-byte aligned): plain, and op with the left and right neighbours
+  static __device__ __forceinline__ void at4(const uint32_t *p, Lanes (&v)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    v[0] = {q.x}; v[1] = {q.y}; v[2] = {q.z}; v[3] = {q.w};
+  }
+  static __device__ __forceinline__ void hor4(const uint32_t *p, Lanes (&h)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t w[6] = {p[-1], q.x, q.y, q.z, q.w, p[4]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      h[k] = {m16<SUP>(w[k + 1],
+                       m16<SUP>(__funnelshift_l(w[k], w[k + 1], 16), __funnelshift_r(w[k + 1], w[k + 2], 16)))};
   }
   __device__ __forceinline__ Lanes op(Lanes b) const { return {m16<SUP>(w, b.w)}; }
   __device__ __forceinline__ uint32_t word() const { return w; }
@@ -65,6 +82,27 @@ template <bool SUP> struct Lanes<uint8_t, SUP> {
     const uint32_t M = m16<SUP>(E, O);
     return {m16<SUP>(M, __funnelshift_l(Op, O, 16)), m16<SUP>(M, __funnelshift_r(E, En, 16))};
   }
+  static __device__ __forceinline__ void at4(const uint32_t *p, Lanes (&v)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = {__byte_perm(w[k], 0, 0x4240), __byte_perm(w[k], 0, 0x4341)};
+  }
+  // each word split once; the left word's odd and the right word's even pixels from the neighbours
+  static __device__ __forceinline__ void hor4(const uint32_t *p, Lanes (&h)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+    uint32_t E[6], O[6];  // index k + 1 = word k; O[0] of the left word, E[5] of the right one
+    O[0] = __byte_perm(p[-1], 0, 0x4341);
+    E[5] = __byte_perm(p[4], 0, 0x4240);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { E[k + 1] = __byte_perm(w[k], 0, 0x4240); O[k + 1] = __byte_perm(w[k], 0, 0x4341); }
+#pragma unroll
+    for (int k = 1; k <= 4; ++k) {
+      const uint32_t M = m16<SUP>(E[k], O[k]);
+      h[k - 1] = {m16<SUP>(M, __funnelshift_l(O[k - 1], O[k], 16)), m16<SUP>(M, __funnelshift_r(E[k], E[k + 1], 16))};
+    }
+  }
   __device__ __forceinline__ Lanes op(Lanes b) const { return {m16<SUP>(e, b.e), m16<SUP>(o, b.o)}; }
   __device__ __forceinline__ uint32_t word() const { return __byte_perm(e, o, 0x6240); }
 };
@@ -74,6 +112,16 @@ template <typename T, bool SUP> struct Lanes {
   static __device__ __forceinline__ Lanes at(const uint32_t *p) { return {p[0]}; }
   static __device__ __forceinline__ Lanes hor(const uint32_t *p) {
     return {wop<T, SUP>(p[0], wop<T, SUP>(p[-1], p[1]))};
+  }
+  static __device__ __forceinline__ void at4(const uint32_t *p, Lanes (&v)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    v[0] = {q.x}; v[1] = {q.y}; v[2] = {q.z}; v[3] = {q.w};
+  }
+  static __device__ __forceinline__ void hor4(const uint32_t *p, Lanes (&h)[4]) {
+    const uint4 q = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t w[6] = {p[-1], q.x, q.y, q.z, q.w, p[4]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = {wop<T, SUP>(w[k + 1], wop<T, SUP>(w[k], w[k + 2]))};
   }
   __device__ __forceinline__ Lanes op(Lanes b) const { return {wop<T, SUP>(w, b.w)}; }
   __device__ __forceinline__ uint32_t word() const { return w; }
@@ -147,6 +195,68 @@ __global__ void __launch_bounds__(kSTThreads) k_small2d_tile(const __grid_consta
       res = L::hor(p - kSTBW);
     }
     if (i < nrows) dst[(size_t)i * Wn] = res.word();
+  }
+}
+
+// The same tile of 64 words, kST2QRows rows high, with a thread per 16-byte quad of words and
+// kST2QRows / 16 rows: each box row is read as one 16-byte load plus the two neighbouring words, each
+// u8 word split once (not three times, as the centre and as each neighbour's neighbour), and the
+// results stored 16 bytes at a time.
+template <typename T, bool SUP, int SHAPE>
+__global__ void __launch_bounds__(kSTThreads) k_small2d_quad(const __grid_constant__ CUtensorMap tmap,
+                                                            uint32_t *__restrict__ out, int H, int Wn) {
+  using L = Lanes<T, SUP>;
+  constexpr int TH = kST2QRows, BH = TH + 2, QC = kSTW / 4, RPT = TH / (kSTThreads / QC);
+  extern __shared__ __align__(128) uint32_t s_box[];  // [BH][kSTBW] + the mbarrier
+  __shared__ int s_ok;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(s_box + BH * kSTBW);
+  const int wx0 = (int)blockIdx.x * kSTW, y0 = (int)blockIdx.y * TH;
+  const int tx = wx0 - 4, ty = y0 - 1;
+  if (!load_tile(&tmap, s_box, bar, (unsigned)(BH * kSTBW * 4), tx, ty, &g_small_tile_status, &s_ok)) return;
+  if constexpr (!(SUP && std::is_unsigned_v<T>)) {
+    if (tx < 0 || tx + kSTBW > Wn || ty < 0 || ty + BH > H)
+      fill_outside(s_box, BH, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
+                   [&](int r) { return ty + r >= 0 && ty + r < H; });
+  }
+
+  const int q = threadIdx.x % QC, g = threadIdx.x / QC;
+  const int gw = wx0 + 4 * q;  // first word of the quad (Wn is a multiple of 4: quads are whole)
+  if (gw >= Wn) return;
+  const int r0 = g * RPT;
+  const int nrows = min(RPT, H - (y0 + r0));
+  if (nrows <= 0) return;
+  const uint32_t *col = s_box + 4 + 4 * q + r0 * kSTBW;  // box row r0, the quad's first word
+  uint4 *dst = reinterpret_cast<uint4 *>(out + (size_t)(y0 + r0) * Wn + gw);
+  const size_t pitch = (size_t)Wn / 4;
+  L a[4], b[4];
+  if constexpr (SHAPE == ST_SQUARE) { L::hor4(col, a); L::hor4(col + kSTBW, b); }
+  else if constexpr (SHAPE == ST_CROSS || SHAPE == ST_SEGY) { L::at4(col, a); L::at4(col + kSTBW, b); }
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const uint32_t *p = col + (i + 2) * kSTBW;
+    L res[4], n[4];
+    if constexpr (SHAPE == ST_SQUARE) {
+      L::hor4(p, n);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) res[k] = b[k].op(a[k]).op(n[k]);
+    } else if constexpr (SHAPE == ST_CROSS) {
+      L::at4(p, n);
+      L h[4];
+      L::hor4(p - kSTBW, h);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) res[k] = h[k].op(a[k]).op(n[k]);
+    } else if constexpr (SHAPE == ST_SEGY) {
+      L::at4(p, n);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) res[k] = b[k].op(a[k]).op(n[k]);
+    } else {
+      L::hor4(p - kSTBW, res);
+    }
+    if constexpr (SHAPE != ST_SEGX) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { a[k] = b[k]; b[k] = n[k]; }
+    }
+    if (i < nrows) dst[i * pitch] = make_uint4(res[0].word(), res[1].word(), res[2].word(), res[3].word());
   }
 }
 
@@ -235,10 +345,13 @@ pg_status small2d_tile_t(const pg_image &in, const pg_image &out, cudaStream_t s
   const Dims d = dims_of(in);
   const int64_t H = d.ny, Wn = d.nx * (int64_t)sizeof(T) / 4;
   CUtensorMap map;
-  PG_TRY(word_map(&map, in.data, H, Wn, kSTBW, kST2Rows + 2));
-  constexpr size_t smem = (size_t)(kST2Rows + 2) * kSTBW * 4 + 16;
-  const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, kST2Rows));
-  k_small2d_tile<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)H, (int)Wn);
+  constexpr int TH = kQuad2D<T> ? kST2QRows : kST2Rows;
+  PG_TRY(word_map(&map, in.data, H, Wn, kSTBW, TH + 2));
+  constexpr size_t smem = (size_t)(TH + 2) * kSTBW * 4 + 16;
+  const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, TH));
+  uint32_t *dst = static_cast<uint32_t *>(out.data);
+  if constexpr (kQuad2D<T>) k_small2d_quad<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
+  else k_small2d_tile<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
   return cuda_status(cudaGetLastError(), "small-SE tile launch");
 }
 

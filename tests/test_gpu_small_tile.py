@@ -2,7 +2,8 @@
 rows are a multiple of 16 bytes take them for the 2D and 3D squares and crosses and the X / Y segments
 (the Z segment stays on the slice-streaming kernel); the result must equal
 the oracle's static-SE Erode / Dilate (ero_dil_static.cpp:229-306) bit for bit.  The shapes put the
-tile's columns (64 words: 256 u8 / 128 u16 pixels), its rows (64 in 2D, 16 in 3D), its slices (8) and
+tile's columns (64 words: 256 u8 / 128 u16 pixels), its rows (2D: 128 for u8, a thread per 16-byte quad;
+64 for wider pixels, a thread per word; 3D: 16), its slices (8) and
 the image border in every relative position; constant images at the type's extremes check the neutral
 value outside the image (the erosion's maximum replaces TMA's zero fill)."""
 import ctypes
@@ -17,8 +18,8 @@ pytestmark = pytest.mark.gpu
 
 SES = ["SESquare2D", "SECross2D", "SESegmentX2D", "SESegmentY2D"]
 SES3 = ["SESquare3D", "SECross3D", "SESegmentX3D", "SESegmentY3D", "SESegmentZ3D"]
-SHAPES = {np.uint8: [(1, 16), (2, 32), (3, 16), (63, 48), (64, 256), (65, 272), (66, 512), (129, 1040),
-                     (257, 784)],
+SHAPES = {np.uint8: [(1, 16), (2, 32), (3, 16), (63, 48), (64, 256), (65, 272), (66, 512), (127, 256),
+                     (128, 512), (129, 1040), (130, 272), (257, 784)],
           np.uint16: [(1, 8), (2, 16), (3, 8), (63, 24), (64, 128), (65, 136), (66, 256), (129, 520),
                       (257, 392)]}
 SHAPES3 = {np.uint8: [(1, 1, 16), (1, 3, 32), (2, 17, 48), (8, 16, 256), (9, 15, 272), (10, 18, 64),
