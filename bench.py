@@ -354,7 +354,7 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
                     ms = _time_ms(lambda fn=fn, se=se: fn(x, se, o), flush, 15, 2)
                     rec(f"cfg3_{op}_{sname}_4096_{dt}", ms, x.numel(), 2 * x.numel() * es)
             del x, o
-        # the 3x3 square on a 4096^2 u8 image (the small-SE streaming kernel)
+        # the 3x3 square on a 4096^2 u8 image and the 3x3x3 cube on a 256^3 u8 volume (TMA tile kernels)
         x8 = torch.from_numpy(synthetic.uniform_u8((4096, 4096), 2)).to(dev)
         o8 = torch.empty_like(x8)
         for dil in (True, False):
