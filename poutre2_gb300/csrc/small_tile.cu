@@ -5,8 +5,8 @@
 // Same result as k_small2d / k_small3d (small_se.cu) and the reference's static-SE dispatchers
 // (ero_dil_static_se_t.hpp:298-915): per pixel the min / max over the SE's offsets inside the image.
 //
-// A CTA (256 threads) owns an output tile of 64 32-bit words (4 / sizeof(T) pixels each) by BY rows
-// (by BZ slices for a volume).  One TMA copy brings the box around it -- a 16-byte chunk of halo left
+// A CTA owns an output tile of 64 32-bit words (4 / sizeof(T) pixels each) by 64 rows (a volume's: by
+// 8 rows by 8 slices).  One TMA copy brings the box around it -- a 16-byte chunk of halo left
 // and right, a row above and below, a slice before and after -- into shared memory, so all of the
 // tile's loads are in flight at once; the grids of the usual image sizes fit in one wave of resident
 // CTAs.  A thread owns one word column (or, for u8 images, a 16-byte quad of words) over a run of the
@@ -32,13 +32,15 @@ constexpr int kSTThreads = 256;
 constexpr int kSTW = 64;         // output words per tile row
 constexpr int kSTBW = kSTW + 8;  // box words: one 16-byte chunk of halo each side
 constexpr int kST2Rows = 64;     // output rows of a 2D tile (a thread per word)
-constexpr int kST2QRows = 128;   // output rows of a 2D tile (a thread per quad of words)
+constexpr int kST2QRows = 64;    // output rows of a 2D tile (a thread per quad of words)
 // u8 images take the quad kernel (4096^2 square 12.3 -> 10.2 us); for u16 / i32 / f32 the thread per
 // word measured 1-2 % faster on 8192^2 / 16384^2 images and the same on 4096^2
 template <typename T> constexpr bool kQuad2D = sizeof(T) == 1;
-constexpr int kST3Rows = 16;     // output rows of a 3D tile
-constexpr int kST3Slices = 8;    // output slices of a 3D tile
-enum { ST_SQUARE = 0, ST_CROSS = 1, ST_SEGX = 2, ST_SEGY = 3, ST_SEGZ = 4 };
+constexpr int kST2QThreads = 128;  // threads of a quad tile
+constexpr int kST3Rows = 8;        // output rows of a 3D tile
+constexpr int kST3Slices = 8;      // output slices of a 3D tile
+constexpr int kST3Threads = 128;   // threads of a 3D tile
+enum { ST_SQUARE = 0, ST_CROSS = 1, ST_SEGX = 2, ST_SEGY = 3 };
 
 template <bool SUP> __device__ __forceinline__ uint32_t m16(uint32_t a, uint32_t b) { return wop<uint16_t, SUP>(a, b); }
 
@@ -131,10 +133,10 @@ template <typename T, bool SUP> struct Lanes {
 // unsigned dilations): box rows wholly outside the image (row_in(r) false), and the words left of box
 // word c_lo / from box word c_hi of the others (c_lo, c_hi multiples of 4; box rows of 72 words start
 // on 16-byte boundaries).
-template <typename F>
+template <int NT, typename F>
 __device__ __forceinline__ void fill_outside(uint32_t *box, int nrows, int c_lo, int c_hi, uint32_t neu, F row_in) {
   const uint4 ones = make_uint4(neu, neu, neu, neu);
-  for (int r = threadIdx.x; r < nrows; r += kSTThreads) {
+  for (int r = threadIdx.x; r < nrows; r += NT) {
     uint4 *row = reinterpret_cast<uint4 *>(box + r * kSTBW);
     if (!row_in(r)) {
 #pragma unroll
@@ -160,8 +162,8 @@ __global__ void __launch_bounds__(kSTThreads) k_small2d_tile(const __grid_consta
   if (!load_tile(&tmap, s_box, bar, (unsigned)(BH * kSTBW * 4), tx, ty, &g_small_tile_status, &s_ok)) return;
   if constexpr (!(SUP && std::is_unsigned_v<T>)) {
     if (tx < 0 || tx + kSTBW > Wn || ty < 0 || ty + BH > H)
-      fill_outside(s_box, BH, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
-                   [&](int r) { return ty + r >= 0 && ty + r < H; });
+      fill_outside<kSTThreads>(s_box, BH, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
+                               [&](int r) { return ty + r >= 0 && ty + r < H; });
   }
 
   const int c = threadIdx.x % kSTW, g = threadIdx.x / kSTW;
@@ -198,15 +200,15 @@ __global__ void __launch_bounds__(kSTThreads) k_small2d_tile(const __grid_consta
   }
 }
 
-// The same tile of 64 words, kST2QRows rows high, with a thread per 16-byte quad of words and
-// kST2QRows / 16 rows: each box row is read as one 16-byte load plus the two neighbouring words, each
+// The same tile of 64 words by kST2QRows rows with a thread per 16-byte quad of words and
+// kST2QRows / 8 rows: each box row is read as one 16-byte load plus the two neighbouring words, each
 // u8 word split once (not three times, as the centre and as each neighbour's neighbour), and the
 // results stored 16 bytes at a time.
 template <typename T, bool SUP, int SHAPE>
-__global__ void __launch_bounds__(kSTThreads) k_small2d_quad(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(kST2QThreads) k_small2d_quad(const __grid_constant__ CUtensorMap tmap,
                                                             uint32_t *__restrict__ out, int H, int Wn) {
   using L = Lanes<T, SUP>;
-  constexpr int TH = kST2QRows, BH = TH + 2, QC = kSTW / 4, RPT = TH / (kSTThreads / QC);
+  constexpr int TH = kST2QRows, BH = TH + 2, QC = kSTW / 4, RPT = TH / (kST2QThreads / QC);
   extern __shared__ __align__(128) uint32_t s_box[];  // [BH][kSTBW] + the mbarrier
   __shared__ int s_ok;
   uint64_t *bar = reinterpret_cast<uint64_t *>(s_box + BH * kSTBW);
@@ -215,8 +217,8 @@ __global__ void __launch_bounds__(kSTThreads) k_small2d_quad(const __grid_consta
   if (!load_tile(&tmap, s_box, bar, (unsigned)(BH * kSTBW * 4), tx, ty, &g_small_tile_status, &s_ok)) return;
   if constexpr (!(SUP && std::is_unsigned_v<T>)) {
     if (tx < 0 || tx + kSTBW > Wn || ty < 0 || ty + BH > H)
-      fill_outside(s_box, BH, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
-                   [&](int r) { return ty + r >= 0 && ty + r < H; });
+      fill_outside<kST2QThreads>(s_box, BH, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
+                                 [&](int r) { return ty + r >= 0 && ty + r < H; });
   }
 
   const int q = threadIdx.x % QC, g = threadIdx.x / QC;
@@ -264,12 +266,12 @@ __global__ void __launch_bounds__(kSTThreads) k_small2d_quad(const __grid_consta
 // B(s) = what the slices before and after contribute; out(z) = op(B(z - 1), A(z), B(z + 1)) (B is
 // unused for the X and Y segments).
 template <typename T, bool SUP, int SHAPE>
-__global__ void __launch_bounds__(kSTThreads) k_small3d_tile(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(kST3Threads) k_small3d_tile(const __grid_constant__ CUtensorMap tmap,
                                                             uint32_t *__restrict__ out, int D, int H, int Wn) {
   using L = Lanes<T, SUP>;
   constexpr int BY = kST3Rows, BZ = kST3Slices, RY = BY + 2, RZ = BZ + 2, PL = RY * kSTBW;
-  constexpr int NR = BY / (kSTThreads / kSTW);  // output rows per thread (4)
-  constexpr bool USE_B = SHAPE == ST_SQUARE || SHAPE == ST_CROSS || SHAPE == ST_SEGZ;
+  constexpr int NR = BY / (kST3Threads / kSTW);  // output rows per thread
+  constexpr bool USE_B = SHAPE == ST_SQUARE || SHAPE == ST_CROSS;
   extern __shared__ __align__(128) uint32_t s_box[];  // [RZ][RY][kSTBW] + the mbarrier
   __shared__ int s_ok;
   uint64_t *bar = reinterpret_cast<uint64_t *>(s_box + RZ * PL);
@@ -278,10 +280,11 @@ __global__ void __launch_bounds__(kSTThreads) k_small3d_tile(const __grid_consta
   if (!load_box<3>(&tmap, s_box, bar, (unsigned)(RZ * PL * 4), tx, ty, tz, &g_small_tile_status, &s_ok)) return;
   if constexpr (!(SUP && std::is_unsigned_v<T>)) {
     if (tx < 0 || tx + kSTBW > Wn || ty < 0 || ty + RY > H || tz < 0 || tz + RZ > D)
-      fill_outside(s_box, RZ * RY, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()), [&](int r) {
-        const int s = r / RY, gz = tz + s, gy = ty + (r - s * RY);
-        return gz >= 0 && gz < D && gy >= 0 && gy < H;
-      });
+      fill_outside<kST3Threads>(s_box, RZ * RY, max(0, -tx), min(kSTBW, Wn - tx), splat<T>(Op<T, SUP>::neutral()),
+                                [&](int r) {
+                                  const int s = r / RY, gz = tz + s, gy = ty + (r - s * RY);
+                                  return gz >= 0 && gz < D && gy >= 0 && gy < H;
+                                });
   }
 
   const int c = threadIdx.x % kSTW, g = threadIdx.x / kSTW;
@@ -308,15 +311,12 @@ __global__ void __launch_bounds__(kSTThreads) k_small3d_tile(const __grid_consta
     } else if constexpr (SHAPE == ST_SEGX) {
 #pragma unroll
       for (int j = 0; j < NR; ++j) A[j] = L::hor(p + (j + 1) * kSTBW);
-    } else if constexpr (SHAPE == ST_SEGY) {
+    } else {
       L v[NR + 2];
 #pragma unroll
       for (int i = 0; i < NR + 2; ++i) v[i] = L::at(p + i * kSTBW);
 #pragma unroll
       for (int j = 0; j < NR; ++j) A[j] = v[j + 1].op(v[j]).op(v[j + 2]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < NR; ++j) { A[j] = L::at(p + (j + 1) * kSTBW); B[j] = A[j]; }
     }
   };
   L Ap[NR], Bp[NR], Ac[NR], Bc[NR];
@@ -350,7 +350,7 @@ pg_status small2d_tile_t(const pg_image &in, const pg_image &out, cudaStream_t s
   constexpr size_t smem = (size_t)(TH + 2) * kSTBW * 4 + 16;
   const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, TH));
   uint32_t *dst = static_cast<uint32_t *>(out.data);
-  if constexpr (kQuad2D<T>) k_small2d_quad<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
+  if constexpr (kQuad2D<T>) k_small2d_quad<T, SUP, SHAPE><<<grid, kST2QThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
   else k_small2d_tile<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
   return cuda_status(cudaGetLastError(), "small-SE tile launch");
 }
@@ -366,7 +366,7 @@ pg_status small3d_tile_t(const pg_image &in, const pg_image &out, cudaStream_t s
       cudaFuncSetAttribute(k_small3d_tile<T, SUP, SHAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   PG_CUDA_TRY(attr, "small-SE volume tile smem attribute");
   const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, kST3Rows), (unsigned)ceil_div(D, kST3Slices));
-  k_small3d_tile<T, SUP, SHAPE><<<grid, kSTThreads, smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)D, (int)H,
+  k_small3d_tile<T, SUP, SHAPE><<<grid, kST3Threads, smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)D, (int)H,
                                                               (int)Wn);
   return cuda_status(cudaGetLastError(), "small-SE volume tile launch");
 }
@@ -381,8 +381,7 @@ pg_status small_tile_se(const pg_image &in, const pg_image &out, int se, cudaStr
     case PG_SE_SQUARE_3D: return small3d_tile_t<T, SUP, ST_SQUARE>(in, out, s);
     case PG_SE_CROSS_3D: return small3d_tile_t<T, SUP, ST_CROSS>(in, out, s);
     case PG_SE_SEGMENT_X_3D: return small3d_tile_t<T, SUP, ST_SEGX>(in, out, s);
-    case PG_SE_SEGMENT_Y_3D: return small3d_tile_t<T, SUP, ST_SEGY>(in, out, s);
-    default: return small3d_tile_t<T, SUP, ST_SEGZ>(in, out, s);
+    default: return small3d_tile_t<T, SUP, ST_SEGY>(in, out, s);  // PG_SE_SEGMENT_Y_3D
   }
 }
 

@@ -2,8 +2,8 @@
 rows are a multiple of 16 bytes take them for the 2D and 3D squares and crosses and the X / Y segments
 (the Z segment stays on the slice-streaming kernel); the result must equal
 the oracle's static-SE Erode / Dilate (ero_dil_static.cpp:229-306) bit for bit.  The shapes put the
-tile's columns (64 words: 256 u8 / 128 u16 pixels), its rows (2D: 128 for u8, a thread per 16-byte quad;
-64 for wider pixels, a thread per word; 3D: 16), its slices (8) and
+tile's columns (64 words: 256 u8 / 128 u16 pixels), its rows (2D: 64, with a thread per 16-byte quad for
+u8 and per word for wider pixels; 3D: 8), its slices (8) and
 the image border in every relative position; constant images at the type's extremes check the neutral
 value outside the image (the erosion's maximum replaces TMA's zero fill)."""
 import ctypes
