@@ -348,6 +348,7 @@ pg_status small2d_tile_t(const pg_image &in, const pg_image &out, cudaStream_t s
   constexpr int TH = kQuad2D<T> ? kST2QRows : kST2Rows;
   PG_TRY(word_map(&map, in.data, H, Wn, kSTBW, TH + 2));
   constexpr size_t smem = (size_t)(TH + 2) * kSTBW * 4 + 16;
+  static_assert(smem <= 48 * 1024, "above 48 KB the kernel needs the dynamic shared memory attribute");
   const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, TH));
   uint32_t *dst = static_cast<uint32_t *>(out.data);
   if constexpr (kQuad2D<T>) k_small2d_quad<T, SUP, SHAPE><<<grid, kST2QThreads, smem, s>>>(map, dst, (int)H, (int)Wn);
@@ -362,9 +363,7 @@ pg_status small3d_tile_t(const pg_image &in, const pg_image &out, cudaStream_t s
   CUtensorMap map;
   PG_TRY(word_map3(&map, in.data, D, H, Wn, kSTBW, kST3Rows + 2, kST3Slices + 2));
   constexpr size_t smem = (size_t)(kST3Slices + 2) * (kST3Rows + 2) * kSTBW * 4 + 16;
-  static const cudaError_t attr =  // once per kernel (thread-safe static initialisation)
-      cudaFuncSetAttribute(k_small3d_tile<T, SUP, SHAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  PG_CUDA_TRY(attr, "small-SE volume tile smem attribute");
+  static_assert(smem <= 48 * 1024, "above 48 KB the kernel needs the dynamic shared memory attribute");
   const dim3 grid((unsigned)ceil_div(Wn, kSTW), (unsigned)ceil_div(H, kST3Rows), (unsigned)ceil_div(D, kST3Slices));
   k_small3d_tile<T, SUP, SHAPE><<<grid, kST3Threads, smem, s>>>(map, static_cast<uint32_t *>(out.data), (int)D, (int)H,
                                                               (int)Wn);
