@@ -366,6 +366,9 @@ def extra_measurements(dev, flush, only=None, cfg5_batch=64):
         for dil in (True, False):
             ms = _time_ms(lambda d=dil: (llm.Dilate if d else llm.Erode)(v, Common_NL_SE.SESquare3D, 1, o), flush, 15, 3)
             rec(f"cfg3_{'dilate' if dil else 'erode'}_cube3_256_u8", ms, v.numel(), 2 * v.numel())
+        # the event bracket's own floor: a 16-element add timed the same way (part of every row above)
+        z = torch.zeros(16, device=dev)
+        res["event_floor_add16_us"] = round(_time_ms(lambda: z.add_(1), flush, 15, 3) * 1e3, 2)
 
     def large():
         # 16384^2 u16 (512 MiB in, 512 MiB out): the output is four times the 129 MB L2, so the
